@@ -1,0 +1,359 @@
+#!/usr/bin/env python3
+"""Benchmark of the GB300 muon DCS path (one JSON line on stdout, rank 0).
+
+Workload (one "step"): the four DCS processes of NOA's PMS module --
+bremsstrahlung, pair production, photonuclear, ionisation -- evaluated in
+plain FP64 over 1e7 seeded (K, q) pairs of standard rock for a muon, i.e.
+4e7 DCS evaluations.  This is the reference's benchmark of
+benchmark/measure-dcs-calc.cc (vectorised dcs::vmap per process) at the
+1e7-pair configuration; the pairs follow K ~ log-uniform[1e-3, 1e6] GeV,
+nu ~ log-uniform[1e-7, 1], q = nu K (noa_gb300.workload, seed 987654).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+`value` is DCS evaluations per second with inputs resident in HBM (CUDA
+events on the launching stream; K and q are 160 MB, above the 129 MB L2, so
+no flush is needed between steps).  `e2e` is the same metric through the C
+ABI's host-buffer entry point (noa_dcs_vmap_host) from pinned host memory,
+copies included.  `--impl reference` times the reference algorithm on the
+host cores instead (the CPU oracle, an operation-for-operation restatement of
+src/noa/pms/dcs.hh, OpenMP over all cores like dcs::pvmap).
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "DCS evals/sec per process on 1 GB300 (plain FP64 vs FP32-comp vs MLP) at stated rel. error"
+PROCESSES = ("bremsstrahlung", "pair_production", "photonuclear", "ionisation")
+N_PAIRS = 10_000_000
+# Algorithmic work per evaluation on this workload, in flop-equivalents
+# (+ - * / sqrt compare = 1, log exp pow log10 = 20), counted by running the
+# reference's operation sequence on an op-counting scalar over 1e6 pairs of
+# the seeded law (tests/test_bench_contract.py re-derives them).
+FLOP_EQ_PER_EVAL = {"bremsstrahlung": 156.27, "pair_production": 1192.49,
+                    "photonuclear": 949.69, "ionisation": 57.98}
+BYTES_PER_EVAL = 24  # K and q read, result written, float64
+
+
+def parse_args():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--n", type=int, default=N_PAIRS)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    return ap.parse_args()
+
+
+def dist_env():
+    return (int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)),
+            int(os.environ.get("LOCAL_RANK", 0)))
+
+
+# ---------------------------------------------------------------- CPU side
+def cpu_reference_rate(n_sample, reps=3, offset=0):
+    """Evaluations/s of the oracle (reference algorithm) with every host
+    thread, on the first n_sample pairs of the workload, all four processes."""
+    import oracle
+    from noa_gb300.elements import MUON_MASS, STANDARD_ROCK
+    from noa_gb300.workload import kinetic_recoil
+    K, q = kinetic_recoil(n_sample, offset=offset)
+    per = {}
+    total_t = []
+    for _ in range(reps):
+        t_all = 0.0
+        for p, name in enumerate(PROCESSES):
+            t0 = time.perf_counter()
+            oracle.dcs(p, K, q, STANDARD_ROCK, MUON_MASS, threads=0)
+            dt = time.perf_counter() - t0
+            per.setdefault(name, []).append(dt)
+            t_all += dt
+        total_t.append(t_all)
+    t = statistics.median(total_t)
+    return {
+        "value": 4 * n_sample / t,
+        "seconds_per_sample": t,
+        "per_process": {k: n_sample / statistics.median(v) for k, v in per.items()},
+        "cores": oracle.lib().oracle_max_threads(),
+    }
+
+
+def run_reference(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return
+    n_sample = min(args.n, 2_000_000)
+    import oracle
+    from noa_gb300.elements import MUON_MASS, STANDARD_ROCK
+    from noa_gb300.workload import kinetic_recoil
+    K, q = kinetic_recoil(n_sample)
+    for _ in range(args.warmup):
+        for p in range(4):
+            oracle.dcs(p, K, q, STANDARD_ROCK, MUON_MASS, threads=0)
+    times = []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        for p in range(4):
+            oracle.dcs(p, K, q, STANDARD_ROCK, MUON_MASS, threads=0)
+        times.append(time.perf_counter() - t0)
+    total = sum(times)
+    value = 4 * n_sample * args.steps / total
+    cores = oracle.lib().oracle_max_threads()
+    sample = (f"first {n_sample} pairs of the 1e7-pair workload per step, all four processes "
+              f"(the pairs are i.i.d., so the rate is the workload's)")
+    line = {
+        "metric": METRIC, "value": value, "unit": "evals/s", "impl": "reference", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * total / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic: seeded log-uniform K in [1e-3,1e6] GeV, nu in [1e-7,1], q = nu K",
+        "config": config_dict(args.n, world),
+        "cpu_baseline": {"value": value, "unit": "evals/s", "cores": cores, "kind": "port", "sample": sample},
+        "e2e": {"value": value, "unit": "evals/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def config_dict(n, world):
+    return {"workload": f"plain FP64 DCS, 4 processes x {n:.0e} (K,q) pairs, standard rock, muon",
+            "n_pairs_per_gpu": n, "processes": list(PROCESSES),
+            "element": {"A": 22.0, "I": 0.1364e-6, "Z": 11}, "mass": 0.10565839,
+            "parallelism": f"replicas x{world} (independent shards)" if world > 1 else "single GPU",
+            "l2": "inputs 160 MB > 129 MB L2: no flush between steps"}
+
+
+# ---------------------------------------------------------------- clocks
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled during the timed region."""
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+             "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+             "clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={q}",
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.lines:
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 7:
+                continue
+            try:
+                sm.append(float(f[0]))
+                mx.append(float(f[1]))
+            except ValueError:
+                continue
+            for name, v in zip(names, f[3:7]):
+                if v.lower() == "active":
+                    reasons.add(name)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+# ---------------------------------------------------------------- GPU side
+def measure_fp64_peak(lib, torch, stream):
+    """FP64 FMA-chain throughput (TFLOP/s) of this GPU: the roofline denominator."""
+    import ctypes
+    sms = torch.cuda.get_device_properties(0).multi_processor_count
+    blocks = sms * 8
+    out = torch.empty(blocks * 256, dtype=torch.float64, device="cuda")
+    flops = ctypes.c_double()
+    best = 0.0
+    for it in (64, 2048, 2048, 2048):
+        s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        s.record(stream)
+        rc = lib.noa_dcs_probe_fma(1, out.data_ptr(), blocks, it, ctypes.byref(flops), stream.cuda_stream)
+        e.record(stream)
+        e.synchronize()
+        if rc == 0 and it > 64:
+            best = max(best, flops.value / (s.elapsed_time(e) * 1e-3) / 1e12)
+    return best
+
+
+def load_traffic():
+    path = os.path.join(ROOT, "profiles", "traffic.json")
+    try:
+        with open(path) as f:
+            return json.load(f)
+    except (OSError, ValueError):
+        return {}
+
+
+def run_ours(args):
+    import torch
+    import torch.distributed as tdist
+    from noa_gb300 import _lib
+    from noa_gb300.elements import MUON_MASS, STANDARD_ROCK
+    from noa_gb300.workload import kinetic_recoil
+
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    if world > 1:
+        tdist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    lib = _lib.load()
+    n = args.n
+    K, q = kinetic_recoil(n, offset=rank * n)  # each rank its own shard: weak scaling
+    dev = torch.device("cuda", local)
+    tk = torch.from_numpy(K).to(dev)
+    tq = torch.from_numpy(q).to(dev)
+    outs = [torch.empty_like(tk) for _ in PROCESSES]
+    el = _lib.element_struct(STANDARD_ROCK)
+    stream = torch.cuda.current_stream(dev)
+    sptr = stream.cuda_stream
+
+    def step(ev=None):
+        for p in range(4):
+            if ev is not None:
+                ev[p][0].record(stream)
+            _lib.check(lib.noa_dcs_cuda_vmap(p, 0, outs[p].data_ptr(), tk.data_ptr(), tq.data_ptr(), n, el,
+                                             MUON_MASS, sptr))
+            if ev is not None:
+                ev[p][1].record(stream)
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+
+    evs = [[[torch.cuda.Event(enable_timing=True) for _ in range(2)] for _ in range(4)]
+           for _ in range(args.steps)]
+    start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    if world > 1:
+        tdist.barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clocks:
+        start.record(stream)
+        for s in range(args.steps):
+            step(evs[s])
+        end.record(stream)
+        torch.cuda.synchronize()
+    if world > 1:
+        tdist.barrier()
+    elapsed = start.elapsed_time(end) * 1e-3
+    per_proc_s = {name: sum(evs[s][p][0].elapsed_time(evs[s][p][1]) for s in range(args.steps)) * 1e-3
+                  for p, name in enumerate(PROCESSES)}
+    if world > 1:
+        t = torch.tensor([elapsed], device=dev, dtype=torch.float64)
+        tdist.all_reduce(t, op=tdist.ReduceOp.MAX)
+        elapsed = float(t.item())
+    value = world * 4 * n * args.steps / elapsed
+
+    # e2e: host buffers in pinned memory, through noa_dcs_vmap_host, copies timed.
+    e2e = None
+    if not args.no_e2e:
+        hk = torch.from_numpy(K).pin_memory()
+        hq = torch.from_numpy(q).pin_memory()
+        hout = [torch.empty(n, dtype=torch.float64).pin_memory() for _ in PROCESSES]
+
+        def host_step():
+            for p in range(4):
+                _lib.check(lib.noa_dcs_vmap_host(p, 0, hout[p].data_ptr(), hk.data_ptr(), hq.data_ptr(), n, el,
+                                                 MUON_MASS))
+        host_step()
+        e2e_steps = max(1, min(args.steps, 5))
+        if world > 1:
+            tdist.barrier()
+        t0 = time.perf_counter()
+        for _ in range(e2e_steps):
+            host_step()
+        t_e2e = time.perf_counter() - t0
+        if world > 1:
+            t = torch.tensor([t_e2e], device=dev, dtype=torch.float64)
+            tdist.all_reduce(t, op=tdist.ReduceOp.MAX)
+            t_e2e = float(t.item())
+        e2e = {"value": world * 4 * n * e2e_steps / t_e2e, "unit": "evals/s",
+               "h2d_bytes_per_step": 4 * 2 * 8 * n, "d2h_bytes_per_step": 4 * 8 * n, "steps": e2e_steps,
+               "path": "noa_dcs_vmap_host (pinned host buffers, chunked copy/compute pipeline)"}
+        # correctness of the timed e2e results against the device path
+        for p in range(4):
+            if not torch.equal(hout[p], outs[p].cpu()):
+                raise RuntimeError(f"e2e result differs from device result for {PROCESSES[p]}")
+
+    if rank != 0:
+        if world > 1:
+            tdist.destroy_process_group()
+        return
+
+    peak = measure_fp64_peak(lib, torch, stream)
+    dom = max(per_proc_s, key=per_proc_s.get)
+    dom_launch_s = per_proc_s[dom] / args.steps
+    achieved = FLOP_EQ_PER_EVAL[dom] * n / dom_launch_s / 1e12
+    traffic = load_traffic().get(f"{dom}_fp64_1e7")
+    per_process = {name: {"evals_per_s": n * args.steps / t, "ms_per_launch": 1e3 * t / args.steps,
+                          "flop_eq_tflops": FLOP_EQ_PER_EVAL[name] * n * args.steps / t / 1e12,
+                          "hbm_gbs": BYTES_PER_EVAL * n * args.steps / t / 1e9}
+                   for name, t in per_proc_s.items()}
+    line = {
+        "metric": METRIC, "value": value, "unit": "evals/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1e3 * elapsed / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic: seeded log-uniform K in [1e-3,1e6] GeV, nu in [1e-7,1], q = nu K",
+        "config": config_dict(n, world),
+        "roofline": {"bound": "fp64", "kernel": f"{dom} FP64", "achieved": achieved, "peak": peak,
+                     "unit": "TFLOP/s", "frac": achieved / peak if peak else None,
+                     "traffic": traffic,
+                     "peak_source": "FP64 FMA-chain probe (noa_dcs_probe_fma) measured in this run",
+                     "numerator": f"{FLOP_EQ_PER_EVAL[dom]} flop-eq/eval x {n} evals per launch"},
+        "per_process": per_process,
+        "e2e": e2e,
+        "clocks": clocks.summary(),
+        "gpu_launches": 4 * args.steps,
+    }
+    if not args.no_cpu_baseline and world == 1:
+        cb = cpu_reference_rate(min(n, 1_000_000))
+        line["cpu_baseline"] = {"value": cb["value"], "unit": "evals/s", "cores": cb["cores"], "kind": "port",
+                                "sample": "first 1e6 pairs of the workload, all four processes, median of 3",
+                                "per_process": cb["per_process"]}
+    print(json.dumps(line), flush=True)
+    if world > 1:
+        tdist.destroy_process_group()
+
+
+def main():
+    args = parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,121 @@
+/*
+ * noa_dcs.h -- C ABI of the GB300 muon differential-cross-section (DCS) library.
+ *
+ * Drop-in for the GPU surface of NOA's PMS DCS, noa::pms::dcs::cuda
+ * (grinisrit/noa src/noa/pms/dcs.hh:1004-1019, implemented in
+ * src/noa/pms/dcs.cuh:30-50), which the reference provides for bremsstrahlung
+ * only.  Every entry point takes plain pointers and sizes, never throws, never
+ * aborts, and returns a noa_dcs_status.  A C++/LibTorch layer
+ * (include/noa_gb300/dcs_cuda.hh) and the Python package sit on top of it.
+ *
+ * Memory and streams: unless a function says otherwise, K, q and result are
+ * float64 DEVICE buffers of n elements on the current CUDA device, each
+ * 8-byte aligned; result may be the same buffer as K or q (each element is
+ * read before it is written) but must not partially overlap either.  Work is
+ * enqueued on `stream` (a cudaStream_t; NULL = legacy default stream) and the
+ * call returns without synchronising, like the reference's launch
+ * (src/noa/utils/common.cuh:45-56).  n == 0 is a no-op.
+ */
+#ifndef NOA_DCS_H
+#define NOA_DCS_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define NOA_DCS_ABI_VERSION 1
+
+/* Mirrors noa::pms::AtomicElement (src/noa/pms/physics.hh:39-43):
+ * A in g/mol, I (mean excitation energy) in GeV, Z the charge number.
+ * Same member order and size (24 bytes, 4 trailing pad bytes). */
+typedef struct noa_dcs_element {
+    double A;
+    double I;
+    int32_t Z;
+} noa_dcs_element;
+
+/* The four processes: physics.hh:114-153, dcs.hh:144-258, dcs.hh:362-405,
+ * dcs.hh:408-443. */
+typedef enum noa_dcs_process {
+    NOA_DCS_BREMSSTRAHLUNG = 0,
+    NOA_DCS_PAIR_PRODUCTION = 1,
+    NOA_DCS_PHOTONUCLEAR = 2,
+    NOA_DCS_IONISATION = 3
+} noa_dcs_process;
+
+/* Arithmetic of a launch.  FP64 is the drop-in: it matches the reference's
+ * FP64 CPU path to a mean relative error below 1e-12.  FP32C runs the
+ * quadrature bodies in FP32 with compensated node sums and keeps FP64 at the
+ * kinematic edges; its error bound is stated per process by the tests. */
+typedef enum noa_dcs_precision {
+    NOA_DCS_FP64 = 0,
+    NOA_DCS_FP32C = 1
+} noa_dcs_precision;
+
+typedef enum noa_dcs_status {
+    NOA_DCS_SUCCESS = 0,
+    NOA_DCS_ERROR_INVALID_VALUE = 1,     /* bad process / precision / n < 0 / null pointer */
+    NOA_DCS_ERROR_INVALID_ELEMENT = 2,   /* A or I not finite and positive, or Z < 1 */
+    NOA_DCS_ERROR_MISALIGNED = 3,        /* a buffer is not 8-byte aligned */
+    NOA_DCS_ERROR_NOT_DEVICE_MEMORY = 4, /* a buffer is not device memory of the current device */
+    NOA_DCS_ERROR_OVERLAP = 5,           /* result partially overlaps K or q */
+    NOA_DCS_ERROR_CUDA = 6,              /* a CUDA runtime call failed; see noa_dcs_last_error() */
+    NOA_DCS_ERROR_TIMEOUT = 7,           /* a bounded device-side wait expired */
+    NOA_DCS_ERROR_NOT_SUPPORTED = 8      /* combination not built (e.g. FP32C for ionisation) */
+} noa_dcs_status;
+
+/* ---- per-process entry points: the functions a binding of
+ * noa::pms::dcs::cuda::vmap_<process> (dcs.hh:1004-1010, dcs.cuh:30-41)
+ * calls.  result[i] = dcs(K[i], q[i], element, mass) in FP64. */
+int noa_dcs_cuda_vmap_bremsstrahlung(double *result, const double *K, const double *q, int64_t n,
+                                     const noa_dcs_element *element, double mass, void *stream);
+int noa_dcs_cuda_vmap_pair_production(double *result, const double *K, const double *q, int64_t n,
+                                      const noa_dcs_element *element, double mass, void *stream);
+int noa_dcs_cuda_vmap_photonuclear(double *result, const double *K, const double *q, int64_t n,
+                                   const noa_dcs_element *element, double mass, void *stream);
+int noa_dcs_cuda_vmap_ionisation(double *result, const double *K, const double *q, int64_t n,
+                                 const noa_dcs_element *element, double mass, void *stream);
+
+/* Generic form of the four above with a precision selector.  Replaces the
+ * dispatch a caller would otherwise write over dcs::vmap(dcs::<process>)
+ * (dcs.hh:35-48). */
+int noa_dcs_cuda_vmap(int process, int precision, double *result, const double *K, const double *q, int64_t n,
+                      const noa_dcs_element *element, double mass, void *stream);
+
+/* Host-buffer form: K, q and result are HOST buffers (pinned memory gives
+ * copy/compute overlap; pageable memory works but serialises the copies).
+ * The call stages the data through device buffers owned by the library,
+ * pipelining host-to-device copies, kernels and device-to-host copies in
+ * chunks on its own streams, and returns when result is complete.  This is the
+ * GPU counterpart of calling dcs::vmap / dcs::pvmap on CPU tensors
+ * (dcs.hh:35-75). */
+int noa_dcs_vmap_host(int process, int precision, double *result, const double *K, const double *q, int64_t n,
+                      const noa_dcs_element *element, double mass);
+
+/* Frees the host-path staging buffers of the current device (they are
+ * otherwise kept for reuse until the process exits). */
+int noa_dcs_release_staging(void);
+
+/* Human-readable name of a status code (static storage). */
+const char *noa_dcs_status_string(int status);
+
+/* Message of the last failed call on this host thread ("" if none). */
+const char *noa_dcs_last_error(void);
+
+/* NOA_DCS_ABI_VERSION of the loaded library. */
+int noa_dcs_abi_version(void);
+
+/* Arithmetic-throughput probe (no counterpart in the reference): launches
+ * `blocks` x 256 threads of independent FMA chains in FP64 (fp64 != 0) or
+ * FP32 on `stream`, writing one value per thread to the device buffer `out`,
+ * and stores the launch's flop count in *flops.  Timing it gives the measured
+ * FP64 / FP32 pipe peaks that the DCS kernels' rooflines are quoted against. */
+int noa_dcs_probe_fma(int fp64, void *out, int blocks, int iters, double *flops, void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* NOA_DCS_H */

@@ -1,0 +1,111 @@
+"""Build recipe for the native parts of noa_gb300 (no cmake, no torch headers).
+
+    python -m noa_gb300.build            # CUDA library + CPU oracle
+    python -m noa_gb300.build --ref      # also the reference oracle (needs a noa checkout)
+
+Products (all git-ignored, built in place):
+    noa_gb300/libnoa_dcs.so      CUDA kernels + C ABI of include/noa_dcs.h, sm_103a only
+    oracle/liboracle_dcs.so      CPU restatement used by the tests as the checker
+    oracle/_ref/libnoa_ref_dcs.so  the reference's own dcs.hh (only where a noa checkout exists)
+
+Each .cu file is compiled in its own nvcc process, in parallel, then linked.
+"""
+import concurrent.futures as cf
+import os
+import shutil
+import subprocess
+import sys
+
+PKG = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(PKG)
+CSRC = os.path.join(PKG, "csrc")
+BUILD = os.path.join(PKG, "_build")
+LIB = os.path.join(PKG, "libnoa_dcs.so")
+ORACLE_DIR = os.path.join(ROOT, "oracle")
+ORACLE_LIB = os.path.join(ORACLE_DIR, "liboracle_dcs.so")
+REF_LIB = os.path.join(ORACLE_DIR, "_ref", "libnoa_ref_dcs.so")
+
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+NVCC_FLAGS = ARCH + ["-O3", "-std=c++17", "-lineinfo", "--expt-relaxed-constexpr",
+                     "-Xcompiler", "-fPIC,-ffp-contract=off", "-I", os.path.join(ROOT, "include")]
+
+
+def _nvcc():
+    for cand in (shutil.which("nvcc"), "/usr/local/cuda/bin/nvcc"):
+        if cand and os.path.exists(cand):
+            return cand
+    raise RuntimeError("nvcc not found")
+
+
+def _run(cmd):
+    r = subprocess.run(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("command failed:\n  " + " ".join(cmd) + "\n" + r.stdout)
+    return r.stdout
+
+
+def sources():
+    return sorted(os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith(".cu"))
+
+
+def _stale(target, deps):
+    if not os.path.exists(target):
+        return True
+    t = os.path.getmtime(target)
+    return any(os.path.getmtime(d) > t for d in deps)
+
+
+def _headers():
+    hs = [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".h", ".cuh"))]
+    return hs + [os.path.join(ROOT, "include", "noa_dcs.h")]
+
+
+def build_cuda(verbose=False):
+    nvcc = _nvcc()
+    os.makedirs(BUILD, exist_ok=True)
+    srcs = sources()
+    hdrs = _headers()
+    objs = [os.path.join(BUILD, os.path.basename(s)[:-3] + ".o") for s in srcs]
+    jobs = [(s, o) for s, o in zip(srcs, objs) if _stale(o, [s] + hdrs)]
+    with cf.ThreadPoolExecutor(max_workers=max(1, min(len(jobs), os.cpu_count() or 4))) as ex:
+        outs = list(ex.map(lambda so: _run([nvcc] + NVCC_FLAGS + ["-c", so[0], "-o", so[1]]), jobs))
+    if verbose:
+        for o in outs:
+            sys.stdout.write(o)
+    if jobs or _stale(LIB, objs):
+        _run([nvcc] + ARCH + ["-shared", "-o", LIB] + objs + ["-lcuda"])
+    return LIB
+
+
+def build_oracle():
+    src = os.path.join(ORACLE_DIR, "dcs_oracle.cpp")
+    hdr = os.path.join(ORACLE_DIR, "dcs_oracle.hpp")
+    if _stale(ORACLE_LIB, [src, hdr]):
+        _run(["g++", "-std=c++17", "-O2", "-ffp-contract=off", "-fno-fast-math", "-fopenmp", "-fPIC",
+              "-shared", src, "-o", ORACLE_LIB])
+    return ORACLE_LIB
+
+
+def build_ref(noa_checkout="/root/reference"):
+    """Compiles the reference's own dcs.hh behind oracle/ref_dcs_wrapper.cc.
+    Skipped (returns None) where no noa checkout is present."""
+    if not os.path.exists(os.path.join(noa_checkout, "src", "noa", "pms", "dcs.hh")):
+        return None
+    deps = [os.path.join(ORACLE_DIR, "ref_dcs_wrapper.cc")]
+    if _stale(REF_LIB, deps):
+        _run(["bash", os.path.join(ORACLE_DIR, "build_ref.sh"), noa_checkout])
+    return REF_LIB
+
+
+def build_all(ref=True, verbose=False):
+    with cf.ThreadPoolExecutor(max_workers=3) as ex:
+        f_cuda = ex.submit(build_cuda, verbose)
+        f_oracle = ex.submit(build_oracle)
+        f_ref = ex.submit(build_ref) if ref else None
+        out = {"cuda": f_cuda.result(), "oracle": f_oracle.result()}
+        out["ref"] = f_ref.result() if f_ref else None
+    return out
+
+
+if __name__ == "__main__":
+    print(build_all(ref="--ref" in sys.argv, verbose="-v" in sys.argv))

@@ -1,0 +1,316 @@
+/*
+ * C ABI of the GB300 muon DCS library (include/noa_dcs.h): argument checks,
+ * per-launch constants, dispatch to the kernels, and the pipelined
+ * host-buffer path.
+ *
+ * The reference checks nothing beyond the dtype check of data_ptr<double>()
+ * (src/noa/pms/dcs.cuh:36, common.cuh:47, 65) and ignores launch errors.
+ * Here every entry point validates its arguments before any launch (a bad
+ * pointer must never reach a kernel), reports CUDA errors as a status, and
+ * never throws or aborts.
+ */
+#include "dcs_launch.h"
+
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstdarg>
+#include <cstdint>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+
+namespace {
+
+thread_local char g_last_error[512] = "";
+
+int fail(int status, const char *fmt, ...) {
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(g_last_error, sizeof g_last_error, fmt, ap);
+    va_end(ap);
+    return status;
+}
+
+int cuda_fail(cudaError_t e, const char *what) {
+    return fail(NOA_DCS_ERROR_CUDA, "%s: %s (%s)", what, cudaGetErrorName(e), cudaGetErrorString(e));
+}
+
+int check_element(const noa_dcs_element *el) {
+    if (!el)
+        return fail(NOA_DCS_ERROR_INVALID_VALUE, "element is NULL");
+    if (!std::isfinite(el->A) || !(el->A > 0.) || !std::isfinite(el->I) || !(el->I > 0.) || el->Z < 1)
+        return fail(NOA_DCS_ERROR_INVALID_ELEMENT, "invalid element A=%g I=%g Z=%d", el->A, el->I, (int)el->Z);
+    return NOA_DCS_SUCCESS;
+}
+
+int check_common(int process, int precision, int64_t n, double mass) {
+    if (process < NOA_DCS_BREMSSTRAHLUNG || process > NOA_DCS_IONISATION)
+        return fail(NOA_DCS_ERROR_INVALID_VALUE, "unknown process %d", process);
+    if (precision != NOA_DCS_FP64 && precision != NOA_DCS_FP32C)
+        return fail(NOA_DCS_ERROR_INVALID_VALUE, "unknown precision %d", precision);
+    if (n < 0)
+        return fail(NOA_DCS_ERROR_INVALID_VALUE, "negative size %lld", (long long)n);
+    if (!std::isfinite(mass) || !(mass > 0.))
+        return fail(NOA_DCS_ERROR_INVALID_VALUE, "invalid particle mass %g", mass);
+    return NOA_DCS_SUCCESS;
+}
+
+bool overlaps_partially(const double *a, const double *b, int64_t n) {
+    if (a == b)
+        return false;
+    const uintptr_t a0 = (uintptr_t)a, a1 = a0 + (uintptr_t)n * 8u;
+    const uintptr_t b0 = (uintptr_t)b, b1 = b0 + (uintptr_t)n * 8u;
+    return a0 < b1 && b0 < a1;
+}
+
+int check_device_buffer(const void *p, const char *name, int device) {
+    if (!p)
+        return fail(NOA_DCS_ERROR_INVALID_VALUE, "%s is NULL", name);
+    if ((uintptr_t)p % 8u)
+        return fail(NOA_DCS_ERROR_MISALIGNED, "%s is not 8-byte aligned", name);
+    cudaPointerAttributes attr;
+    const cudaError_t e = cudaPointerGetAttributes(&attr, p);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return cuda_fail(e, "cudaPointerGetAttributes");
+    }
+    if (attr.type != cudaMemoryTypeDevice && attr.type != cudaMemoryTypeManaged)
+        return fail(NOA_DCS_ERROR_NOT_DEVICE_MEMORY, "%s is not device memory", name);
+    if (attr.type == cudaMemoryTypeDevice && attr.device != device)
+        return fail(NOA_DCS_ERROR_NOT_DEVICE_MEMORY, "%s lives on device %d, current device is %d", name,
+                    attr.device, device);
+    return NOA_DCS_SUCCESS;
+}
+
+int launch(int process, int precision, double *result, const double *K, const double *q, int64_t n,
+           const noa_dcs_consts *c, cudaStream_t stream) {
+    cudaError_t e;
+    if (precision == NOA_DCS_FP64)
+        e = noa_dcs_launch_fp64(process, K, q, result, n, c, stream);
+    else
+        return fail(NOA_DCS_ERROR_NOT_SUPPORTED, "precision %d is not built for process %d", precision, process);
+    if (e != cudaSuccess)
+        return cuda_fail(e, "kernel launch");
+    return NOA_DCS_SUCCESS;
+}
+
+// ---------------------------------------------------------------- host path
+constexpr int64_t kChunk = (int64_t)1 << 21; // pairs per pipeline stage
+constexpr int kSlots = 2;
+constexpr int kMaxDevices = 64;
+
+struct Staging {
+    std::mutex mu;
+    double *buf = nullptr; // kSlots x {K, q, out} x kChunk
+    cudaStream_t st[kSlots] = {nullptr, nullptr};
+};
+Staging g_staging[kMaxDevices];
+
+int staging_acquire(Staging &s) {
+    if (s.buf)
+        return NOA_DCS_SUCCESS;
+    cudaError_t e = cudaMalloc((void **)&s.buf, sizeof(double) * 3 * kSlots * kChunk);
+    if (e != cudaSuccess) {
+        s.buf = nullptr;
+        return cuda_fail(e, "cudaMalloc(staging)");
+    }
+    for (int i = 0; i < kSlots; i++) {
+        e = cudaStreamCreateWithFlags(&s.st[i], cudaStreamNonBlocking);
+        if (e != cudaSuccess)
+            return cuda_fail(e, "cudaStreamCreate");
+    }
+    return NOA_DCS_SUCCESS;
+}
+
+} // namespace
+
+extern "C" {
+
+void noa_dcs_fill_consts(noa_dcs_consts *c, double A, double I, int32_t Z, double mass) {
+    std::memset(c, 0, sizeof *c);
+    const double me = NOA_ELECTRON_MASS;
+    c->A = A;
+    c->I = I;
+    c->mass = mass;
+    c->Z = Z;
+    c->Zd = (double)Z;
+    { // physics.hh:121-133
+        const double sqrte = 1.648721271;
+        c->br_phie_factor = mass / (me * me * sqrte);
+        const double rem = 5.63588E-13 * me / mass;
+        c->br_BZ_n = (Z == 1) ? 202.4 : 182.7 * std::pow((double)Z, -1. / 3.);
+        c->br_BZ_e = (Z == 1) ? 446. : 1429. * std::pow((double)Z, -2. / 3.);
+        c->br_D_n = 1.54 * std::pow(A, 0.27);
+        c->br_dcs_factor = 7.297182E-07 * rem * rem * (double)Z;
+        c->br_half_m2 = 0.5 * mass * mass;
+        c->br_Dn_sqrte_m2 = c->br_D_n * sqrte - 2.;
+        c->br_BZe_mass = c->br_BZ_e * mass;
+    }
+    { // dcs.hh:153-166, 235-241
+        const double sqrte = 1.6487212707;
+        const double Z13 = std::pow((double)Z, 1. / 3.);
+        c->pp_Z13 = Z13;
+        c->pp_kmax_shift = mass * (1. - 0.75 * sqrte * Z13);
+        const double r = mass / me;
+        c->pp_r = r;
+        const double A_ = (Z == 1) ? 202.4 : 183.;
+        c->pp_AZ13 = A_ / Z13;
+        c->pp_cL = 2. * sqrte * me * c->pp_AZ13;
+        c->pp_cLe = 2.25 * Z13 * Z13 / (r * r);
+        c->pp_half_r2 = 0.5 * r * r;
+        c->pp_r2 = r * r;
+        c->pp_r_AZ13 = r * c->pp_AZ13;
+        c->pp_15_Z13 = 1.5 * Z13;
+        c->pp_cZ = 1.794664E-34 * (double)Z;
+        c->pp_gamma1 = (Z == 1) ? 4.4E-05 : 1.95E-05;
+        c->pp_gamma2 = (Z == 1) ? 4.8E-05 : 5.30E-05;
+    }
+    { // dcs.hh:290, 313-315, 370-374
+        const double M = 0.931494, mpi = 0.134977;
+        c->ph_logA = std::log(A);
+        c->ph_a_low = std::exp(-0.1 * std::log(A));
+        c->ph_q_min = mpi * (1.0 + 0.5 * mpi / M);
+        c->ph_log_q02 = std::log(0.52544 / 0.06527);
+    }
+    { // dcs.hh:422, 435-436
+        c->io_Wmin = 0.62 * I;
+        const double m1 = mass - me;
+        c->io_k_rad = 0.5 * m1 * m1 / me;
+    }
+}
+
+int noa_dcs_cuda_vmap(int process, int precision, double *result, const double *K, const double *q, int64_t n,
+                      const noa_dcs_element *element, double mass, void *stream) {
+    g_last_error[0] = '\0';
+    int st = check_common(process, precision, n, mass);
+    if (st)
+        return st;
+    if ((st = check_element(element)))
+        return st;
+    if (n == 0)
+        return NOA_DCS_SUCCESS;
+    int device = 0;
+    cudaError_t e = cudaGetDevice(&device);
+    if (e != cudaSuccess)
+        return cuda_fail(e, "cudaGetDevice");
+    if ((st = check_device_buffer(result, "result", device)) || (st = check_device_buffer(K, "K", device)) ||
+        (st = check_device_buffer(q, "q", device)))
+        return st;
+    if (overlaps_partially(result, K, n) || overlaps_partially(result, q, n))
+        return fail(NOA_DCS_ERROR_OVERLAP, "result partially overlaps an input");
+    noa_dcs_consts c;
+    noa_dcs_fill_consts(&c, element->A, element->I, element->Z, mass);
+    return launch(process, precision, result, K, q, n, &c, (cudaStream_t)stream);
+}
+
+int noa_dcs_cuda_vmap_bremsstrahlung(double *result, const double *K, const double *q, int64_t n,
+                                     const noa_dcs_element *element, double mass, void *stream) {
+    return noa_dcs_cuda_vmap(NOA_DCS_BREMSSTRAHLUNG, NOA_DCS_FP64, result, K, q, n, element, mass, stream);
+}
+
+int noa_dcs_cuda_vmap_pair_production(double *result, const double *K, const double *q, int64_t n,
+                                      const noa_dcs_element *element, double mass, void *stream) {
+    return noa_dcs_cuda_vmap(NOA_DCS_PAIR_PRODUCTION, NOA_DCS_FP64, result, K, q, n, element, mass, stream);
+}
+
+int noa_dcs_cuda_vmap_photonuclear(double *result, const double *K, const double *q, int64_t n,
+                                   const noa_dcs_element *element, double mass, void *stream) {
+    return noa_dcs_cuda_vmap(NOA_DCS_PHOTONUCLEAR, NOA_DCS_FP64, result, K, q, n, element, mass, stream);
+}
+
+int noa_dcs_cuda_vmap_ionisation(double *result, const double *K, const double *q, int64_t n,
+                                 const noa_dcs_element *element, double mass, void *stream) {
+    return noa_dcs_cuda_vmap(NOA_DCS_IONISATION, NOA_DCS_FP64, result, K, q, n, element, mass, stream);
+}
+
+int noa_dcs_vmap_host(int process, int precision, double *result, const double *K, const double *q, int64_t n,
+                      const noa_dcs_element *element, double mass) {
+    g_last_error[0] = '\0';
+    int st = check_common(process, precision, n, mass);
+    if (st)
+        return st;
+    if ((st = check_element(element)))
+        return st;
+    if (n == 0)
+        return NOA_DCS_SUCCESS;
+    if (!result || !K || !q)
+        return fail(NOA_DCS_ERROR_INVALID_VALUE, "NULL buffer");
+    if (overlaps_partially(result, K, n) || overlaps_partially(result, q, n))
+        return fail(NOA_DCS_ERROR_OVERLAP, "result partially overlaps an input");
+    int device = 0;
+    cudaError_t e = cudaGetDevice(&device);
+    if (e != cudaSuccess)
+        return cuda_fail(e, "cudaGetDevice");
+    if (device < 0 || device >= kMaxDevices)
+        return fail(NOA_DCS_ERROR_INVALID_VALUE, "device %d out of range", device);
+    noa_dcs_consts c;
+    noa_dcs_fill_consts(&c, element->A, element->I, element->Z, mass);
+
+    Staging &s = g_staging[device];
+    std::lock_guard<std::mutex> lock(s.mu);
+    if ((st = staging_acquire(s)))
+        return st;
+    for (int64_t off = 0, chunk = 0; off < n; off += kChunk, chunk++) {
+        const int slot = (int)(chunk % kSlots);
+        const int64_t m = (n - off) < kChunk ? (n - off) : kChunk;
+        double *dK = s.buf + (int64_t)slot * 3 * kChunk;
+        double *dQ = dK + kChunk;
+        double *dO = dQ + kChunk;
+        const size_t bytes = sizeof(double) * (size_t)m;
+        if ((e = cudaMemcpyAsync(dK, K + off, bytes, cudaMemcpyDefault, s.st[slot])) != cudaSuccess ||
+            (e = cudaMemcpyAsync(dQ, q + off, bytes, cudaMemcpyDefault, s.st[slot])) != cudaSuccess)
+            return cuda_fail(e, "cudaMemcpyAsync(host to device)");
+        if ((st = launch(process, precision, dO, dK, dQ, m, &c, s.st[slot])))
+            return st;
+        if ((e = cudaMemcpyAsync(result + off, dO, bytes, cudaMemcpyDefault, s.st[slot])) != cudaSuccess)
+            return cuda_fail(e, "cudaMemcpyAsync(device to host)");
+    }
+    for (int i = 0; i < kSlots; i++)
+        if ((e = cudaStreamSynchronize(s.st[i])) != cudaSuccess)
+            return cuda_fail(e, "cudaStreamSynchronize");
+    return NOA_DCS_SUCCESS;
+}
+
+int noa_dcs_release_staging(void) {
+    int device = 0;
+    cudaError_t e = cudaGetDevice(&device);
+    if (e != cudaSuccess)
+        return cuda_fail(e, "cudaGetDevice");
+    if (device < 0 || device >= kMaxDevices)
+        return NOA_DCS_SUCCESS;
+    Staging &s = g_staging[device];
+    std::lock_guard<std::mutex> lock(s.mu);
+    for (int i = 0; i < kSlots; i++)
+        if (s.st[i]) {
+            cudaStreamSynchronize(s.st[i]);
+            cudaStreamDestroy(s.st[i]);
+            s.st[i] = nullptr;
+        }
+    if (s.buf) {
+        cudaFree(s.buf);
+        s.buf = nullptr;
+    }
+    return NOA_DCS_SUCCESS;
+}
+
+const char *noa_dcs_status_string(int status) {
+    switch (status) {
+    case NOA_DCS_SUCCESS: return "success";
+    case NOA_DCS_ERROR_INVALID_VALUE: return "invalid value";
+    case NOA_DCS_ERROR_INVALID_ELEMENT: return "invalid element";
+    case NOA_DCS_ERROR_MISALIGNED: return "misaligned buffer";
+    case NOA_DCS_ERROR_NOT_DEVICE_MEMORY: return "not device memory";
+    case NOA_DCS_ERROR_OVERLAP: return "result partially overlaps an input";
+    case NOA_DCS_ERROR_CUDA: return "CUDA error";
+    case NOA_DCS_ERROR_TIMEOUT: return "device-side wait timed out";
+    case NOA_DCS_ERROR_NOT_SUPPORTED: return "not supported";
+    default: return "unknown status";
+    }
+}
+
+const char *noa_dcs_last_error(void) { return g_last_error; }
+
+int noa_dcs_abi_version(void) { return NOA_DCS_ABI_VERSION; }
+
+} // extern "C"

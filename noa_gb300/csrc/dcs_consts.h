@@ -1,0 +1,79 @@
+/*
+ * Per-(element, mass) constants of the four muon DCS processes.
+ *
+ * The reference recomputes these inside every scalar call (three pow() per
+ * bremsstrahlung evaluation, physics.hh:126-128; pow(Z, 1/3) per pair
+ * production evaluation, dcs.hh:154; log(A) per DRSS call, dcs.hh:313-315).
+ * Here the host computes them once per launch with the same libm calls and the
+ * same operation order, so the values are bit-identical to the ones the
+ * reference's CPU path uses, and the kernels read them from the launch
+ * parameters (constant bank, warp-uniform).
+ *
+ * Host code that fills this struct must be compiled with -ffp-contract=off so
+ * that no product is fused into an addition the reference rounds separately.
+ */
+#pragma once
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Physical constants, physics.hh:54-58, 76. */
+#define NOA_AVOGADRO_NUMBER 6.02214076E+23
+#define NOA_ELECTRON_MASS 0.510998910E-03
+#define NOA_MUON_MASS 0.10565839
+#define NOA_X_FRACTION 5E-02
+
+typedef struct noa_dcs_consts {
+    /* element and particle */
+    double A;
+    double I;
+    double mass;
+    double Zd;      /* (double) Z */
+    int32_t Z;
+    int32_t pad_;
+
+    /* bremsstrahlung, physics.hh:119-133 */
+    double br_phie_factor;  /* mass / (me me sqrte) */
+    double br_BZ_n;         /* Z==1 ? 202.4 : 182.7 Z^-1/3 */
+    double br_BZ_e;         /* Z==1 ? 446   : 1429 Z^-2/3 */
+    double br_D_n;          /* 1.54 A^0.27 */
+    double br_dcs_factor;   /* 7.297182e-7 rem rem Z */
+    double br_half_m2;      /* 0.5 mass mass */
+    double br_Dn_sqrte_m2;  /* D_n sqrte - 2 */
+    double br_BZe_mass;     /* BZ_e mass */
+
+    /* pair production, dcs.hh:148-170 */
+    double pp_Z13;          /* Z^(1/3) */
+    double pp_kmax_shift;   /* mass (1 - 0.75 sqrte Z13) */
+    double pp_r;            /* mass / me */
+    double pp_AZ13;         /* A_ / Z13 */
+    double pp_cL;           /* 2 sqrte me AZ13 */
+    double pp_cLe;          /* 2.25 Z13 Z13 / (r r) */
+    double pp_half_r2;      /* 0.5 r r */
+    double pp_r2;           /* r r */
+    double pp_r_AZ13;       /* r AZ13 */
+    double pp_15_Z13;       /* 1.5 Z13 */
+    double pp_cZ;           /* 1.794664e-34 Z */
+    double pp_gamma1;       /* form-factor constants, dcs.hh:235-241 */
+    double pp_gamma2;
+
+    /* photonuclear, dcs.hh:310-319, 370-375 */
+    double ph_logA;         /* log(A) */
+    double ph_a_low;        /* exp(-0.1 log A), x < 0.0014 branch */
+    double ph_q_min;        /* mpi (1 + 0.5 mpi / M) */
+    double ph_log_q02;      /* log(Q02 / Lambda2), ALLM */
+
+    /* ionisation, dcs.hh:408-443 */
+    double io_Wmin;         /* 0.62 I */
+    double io_k_rad;        /* 0.5 m1 m1 / me, radiative-correction threshold */
+} noa_dcs_consts;
+
+/* Fills c from (A, I, Z, mass) with the reference's expressions. */
+void noa_dcs_fill_consts(noa_dcs_consts *c, double A, double I, int32_t Z, double mass);
+
+#ifdef __cplusplus
+}
+#endif

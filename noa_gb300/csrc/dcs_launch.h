@@ -1,0 +1,19 @@
+/*
+ * Internal launch interface between the C ABI (dcs_capi.cu) and the kernel
+ * translation units.  Not installed; the public surface is include/noa_dcs.h.
+ */
+#pragma once
+
+#include "../../include/noa_dcs.h"
+#include "dcs_consts.h"
+
+#include <cuda_runtime.h>
+
+#define NOA_DCS_PROC_BREMS NOA_DCS_BREMSSTRAHLUNG
+#define NOA_DCS_PROC_PPROD NOA_DCS_PAIR_PRODUCTION
+#define NOA_DCS_PROC_PHOTO NOA_DCS_PHOTONUCLEAR
+#define NOA_DCS_PROC_ION NOA_DCS_IONISATION
+
+/* FP64 kernels (dcs_fp64.cu).  Arguments are already validated. */
+cudaError_t noa_dcs_launch_fp64(int process, const double *K, const double *q, double *out, int64_t n,
+                                const noa_dcs_consts *c, cudaStream_t stream);

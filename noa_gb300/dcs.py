@@ -1,0 +1,103 @@
+"""Python mirror of the reference's GPU DCS surface, noa::pms::dcs::cuda.
+
+Reference: src/noa/pms/dcs.hh:1004-1019 (declarations) and
+src/noa/pms/dcs.cuh:30-50 (bremsstrahlung only).  Here all four processes
+exist, with the reference's argument order (result, kinetic_energies,
+recoil_energies, element, mass) and `map_*` twins that allocate the result
+with zeros_like, as dcs.cuh:43-50 does.  Work is enqueued on PyTorch's current
+CUDA stream without synchronising.
+
+Argument errors raise RuntimeError, as the reference's data_ptr<double>()
+dtype check raises c10::Error; unlike the reference, size, device and
+contiguity are checked too (the reference reads out of bounds or silently
+misreads on those).
+"""
+import torch
+
+from . import _lib
+from .elements import MUON_MASS, STANDARD_ROCK, AtomicElement
+
+__all__ = [
+    "vmap", "map", "vmap_host",
+    "vmap_bremsstrahlung", "vmap_pair_production", "vmap_photonuclear", "vmap_ionisation",
+    "map_bremsstrahlung", "map_pair_production", "map_photonuclear", "map_ionisation",
+]
+
+
+def _check_tensor(t, name, device=None):
+    if not isinstance(t, torch.Tensor):
+        raise RuntimeError(f"{name} must be a torch.Tensor")
+    if t.dtype != torch.float64:
+        raise RuntimeError(f"expected scalar type Double for {name} but found {t.dtype}")
+    if not t.is_cuda:
+        raise RuntimeError(f"{name} must be a CUDA tensor")
+    if device is not None and t.device != device:
+        raise RuntimeError(f"{name} is on {t.device}, expected {device}")
+    if not t.is_contiguous():
+        raise RuntimeError(f"{name} must be contiguous")
+
+
+def _process_id(process):
+    if isinstance(process, str):
+        return _lib.PROCESSES.index(process)
+    return int(process)
+
+
+def vmap(process, result, kinetic_energies, recoil_energies, element=STANDARD_ROCK, mass=MUON_MASS,
+         precision="fp64"):
+    """result[i] = DCS(kinetic_energies[i], recoil_energies[i]) for one process."""
+    lib = _lib.load()
+    _check_tensor(result, "result")
+    _check_tensor(kinetic_energies, "kinetic_energies", result.device)
+    _check_tensor(recoil_energies, "recoil_energies", result.device)
+    n = result.numel()
+    if kinetic_energies.numel() != n or recoil_energies.numel() != n:
+        raise RuntimeError(f"size mismatch: result {n}, kinetic_energies {kinetic_energies.numel()}, "
+                           f"recoil_energies {recoil_energies.numel()}")
+    el = _lib.element_struct(element)
+    with torch.cuda.device(result.device):
+        stream = torch.cuda.current_stream(result.device).cuda_stream
+        _lib.check(lib.noa_dcs_cuda_vmap(_process_id(process), _lib.PRECISIONS[precision],
+                                         result.data_ptr(), kinetic_energies.data_ptr(),
+                                         recoil_energies.data_ptr(), n, el, float(mass), stream))
+    return result
+
+
+def map(process, kinetic_energies, recoil_energies, element=STANDARD_ROCK, mass=MUON_MASS, precision="fp64"):
+    """Allocating twin of vmap (dcs.cuh:43-50)."""
+    result = torch.zeros_like(kinetic_energies)
+    return vmap(process, result, kinetic_energies, recoil_energies, element, mass, precision)
+
+
+def vmap_host(process, result, kinetic_energies, recoil_energies, element=STANDARD_ROCK, mass=MUON_MASS,
+              precision="fp64"):
+    """Host-buffer path (noa_dcs_vmap_host): CPU float64 tensors in and out,
+    staged through the GPU; returns when result is filled."""
+    lib = _lib.load()
+    for t, name in ((result, "result"), (kinetic_energies, "kinetic_energies"),
+                    (recoil_energies, "recoil_energies")):
+        if t.dtype != torch.float64 or t.is_cuda or not t.is_contiguous():
+            raise RuntimeError(f"{name} must be a contiguous float64 CPU tensor")
+    n = result.numel()
+    if kinetic_energies.numel() != n or recoil_energies.numel() != n:
+        raise RuntimeError("size mismatch")
+    el = _lib.element_struct(element)
+    _lib.check(lib.noa_dcs_vmap_host(_process_id(process), _lib.PRECISIONS[precision], result.data_ptr(),
+                                     kinetic_energies.data_ptr(), recoil_energies.data_ptr(), n, el,
+                                     float(mass)))
+    return result
+
+
+def _bind(pid):
+    def _vmap(result, kinetic_energies, recoil_energies, element=STANDARD_ROCK, mass=MUON_MASS):
+        return vmap(pid, result, kinetic_energies, recoil_energies, element, mass)
+
+    def _map(kinetic_energies, recoil_energies, element=STANDARD_ROCK, mass=MUON_MASS):
+        return map(pid, kinetic_energies, recoil_energies, element, mass)
+    return _vmap, _map
+
+
+vmap_bremsstrahlung, map_bremsstrahlung = _bind(_lib.BREMSSTRAHLUNG)
+vmap_pair_production, map_pair_production = _bind(_lib.PAIR_PRODUCTION)
+vmap_photonuclear, map_photonuclear = _bind(_lib.PHOTONUCLEAR)
+vmap_ionisation, map_ionisation = _bind(_lib.IONISATION)

@@ -1,0 +1,132 @@
+"""CPU oracle of the muon DCS path -- TEST INFRASTRUCTURE ONLY.
+
+Python access (ctypes) to oracle/liboracle_dcs.so, the scalar C++
+restatement in dcs_oracle.hpp of the reference's src/noa/pms/dcs.hh and
+physics.hh, and, where it was built (only on a host with a noa checkout), to
+oracle/_ref/libnoa_ref_dcs.so, the reference's own code.  Only tests/,
+__graft_entry__.smoke() and bench.py's CPU baseline may use this package; the
+product (noa_gb300) never imports it.
+"""
+import ctypes
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ORACLE_LIB = os.path.join(HERE, "liboracle_dcs.so")
+REF_LIB = os.path.join(HERE, "_ref", "libnoa_ref_dcs.so")
+
+_P = ctypes.c_void_p
+_D = ctypes.c_double
+_I64 = ctypes.c_int64
+_I32 = ctypes.c_int32
+_INT = ctypes.c_int
+
+_oracle = None
+_ref = None
+
+
+def _ptr(a):
+    return a.ctypes.data_as(_P)
+
+
+def _f64(a):
+    return np.ascontiguousarray(a, dtype=np.float64)
+
+
+def lib():
+    global _oracle
+    if _oracle is None:
+        if not os.path.exists(ORACLE_LIB):
+            raise RuntimeError(f"{ORACLE_LIB} is not built; run `python -m noa_gb300.build`")
+        L = ctypes.CDLL(ORACLE_LIB)
+        L.oracle_dcs_vmap.argtypes = [_INT, _P, _P, _P, _I64, _D, _D, _I32, _D, _INT]
+        L.oracle_dcs_vmap.restype = _INT
+        L.oracle_recoil_integral_vmap.argtypes = [_INT, _INT, _P, _P, _I64, _D, _D, _D, _I32, _D,
+                                                  ctypes.c_uint32, _INT]
+        L.oracle_recoil_integral_vmap.restype = _INT
+        L.oracle_dcs_opcount.argtypes = [_INT, _P, _P, _I64, _D, _D, _I32, _D, _P]
+        L.oracle_dcs_opcount.restype = _D
+        L.oracle_max_threads.restype = _INT
+        _oracle = L
+    return _oracle
+
+
+def ref_available():
+    return os.path.exists(REF_LIB)
+
+
+def ref_lib():
+    global _ref
+    if _ref is None:
+        if not ref_available():
+            raise RuntimeError(f"{REF_LIB} is not built (needs a noa checkout)")
+        L = ctypes.CDLL(REF_LIB)
+        L.ref_dcs_vmap.argtypes = [_INT, _INT, _P, _P, _P, _I64, _D, _D, _I32, _D]
+        L.ref_dcs_vmap.restype = _INT
+        L.ref_recoil_integral_vmap.argtypes = [_INT, _INT, _P, _P, _I64, _D, _D, _D, _I32, _D, _I32]
+        L.ref_recoil_integral_vmap.restype = _INT
+        _ref = L
+    return _ref
+
+
+def dcs(process, K, q, element, mass, threads=0):
+    """Oracle DCS of one process over arrays K, q.  threads: 0 = all OpenMP
+    threads, 1 = the serial loop."""
+    K, q = _f64(K), _f64(q)
+    out = np.empty_like(K)
+    rc = lib().oracle_dcs_vmap(int(process), _ptr(K), _ptr(q), _ptr(out), K.size, float(element.A),
+                               float(element.I), int(element.Z), float(mass), int(threads))
+    if rc:
+        raise ValueError(f"oracle_dcs_vmap failed ({rc})")
+    return out
+
+
+def recoil_integral(process, moment, K, xlow, element, mass, min_points=180, threads=0):
+    """Oracle DEL (moment 0) / CEL (moment 1) recoil integral per K."""
+    K = _f64(K)
+    out = np.empty_like(K)
+    rc = lib().oracle_recoil_integral_vmap(int(process), int(moment), _ptr(K), _ptr(out), K.size, float(xlow),
+                                           float(element.A), float(element.I), int(element.Z), float(mass),
+                                           int(min_points), int(threads))
+    if rc:
+        raise ValueError(f"oracle_recoil_integral_vmap failed ({rc})")
+    return out
+
+
+def opcount(process, K, q, element, mass):
+    """Operation counts {add, mul, div, sqrt, cmp, trans} summed over the pairs."""
+    K, q = _f64(K), _f64(q)
+    c = np.zeros(6)
+    lib().oracle_dcs_opcount(int(process), _ptr(K), _ptr(q), K.size, float(element.A), float(element.I),
+                             int(element.Z), float(mass), _ptr(c))
+    return dict(zip(("add", "mul", "div", "sqrt", "cmp", "trans"), c.tolist()))
+
+
+def ref_dcs(process, K, q, element, mass, parallel=False):
+    """The reference's own dcs::vmap (or dcs::pvmap) -- only where it was built."""
+    K, q = _f64(K), _f64(q)
+    out = np.empty_like(K)
+    rc = ref_lib().ref_dcs_vmap(int(process), int(bool(parallel)), _ptr(K), _ptr(q), _ptr(out), K.size,
+                                float(element.A), float(element.I), int(element.Z), float(mass))
+    if rc:
+        raise ValueError(f"ref_dcs_vmap failed ({rc})")
+    return out
+
+
+def ref_recoil_integral(process, moment, K, xlow, element, mass, min_points=180):
+    K = _f64(K)
+    out = np.empty_like(K)
+    rc = ref_lib().ref_recoil_integral_vmap(int(process), int(moment), _ptr(K), _ptr(out), K.size, float(xlow),
+                                            float(element.A), float(element.I), int(element.Z), float(mass),
+                                            int(min_points))
+    if rc:
+        raise ValueError(f"ref_recoil_integral_vmap failed ({rc})")
+    return out
+
+
+def relative_error(computed, expected):
+    """The reference's metric, common.hh:228-236: mean |c - e| / (c + DBL_MIN)."""
+    c = np.asarray(computed, dtype=np.float64)
+    e = np.asarray(expected, dtype=np.float64)
+    return float(np.mean(np.abs((c - e) / (c + np.finfo(np.float64).tiny))))
