@@ -1,10 +1,12 @@
-"""Build recipe for the native parts of noa_gb300 (no cmake, no torch headers).
+"""Build recipe for the native parts of noa_gb300 (no cmake).
 
     python -m noa_gb300.build            # CUDA library + CPU oracle
     python -m noa_gb300.build --ref      # also the reference oracle (needs a noa checkout)
 
 Products (all git-ignored, built in place):
     noa_gb300/libnoa_dcs.so      CUDA kernels + C ABI of include/noa_dcs.h, sm_103a only
+    noa_gb300/libnoa_dcs_torch.so  LibTorch drop-in (include/noa_gb300/dcs_cuda.hh)
+    noa_gb300/_muons_cuda*.so    Python module mirroring the reference notebook's extension
     oracle/liboracle_dcs.so      CPU restatement used by the tests as the checker
     oracle/_ref/libnoa_ref_dcs.so  the reference's own dcs.hh (only where a noa checkout exists)
 
@@ -77,6 +79,58 @@ def build_cuda(verbose=False):
     return LIB
 
 
+TORCH_LIB = os.path.join(PKG, "libnoa_dcs_torch.so")
+
+
+def _torch_flags():
+    import sysconfig
+    import torch
+    tdir = os.path.dirname(torch.__file__)
+    abi = int(bool(torch._C._GLIBCXX_USE_CXX11_ABI))
+    cuda_inc = os.path.join(os.path.dirname(os.path.dirname(_nvcc())), "include")
+    inc = ["-I", os.path.join(ROOT, "include"), "-I", os.path.join(tdir, "include"),
+           "-I", os.path.join(tdir, "include", "torch", "csrc", "api", "include"), "-I", cuda_inc,
+           "-I", sysconfig.get_paths()["include"]]
+    cflags = ["-std=c++17", "-O2", "-fPIC", f"-D_GLIBCXX_USE_CXX11_ABI={abi}"] + inc
+    libs = ["-L", os.path.join(tdir, "lib"), f"-Wl,-rpath,{os.path.join(tdir, 'lib')}", "-Wl,-rpath,$ORIGIN",
+            "-ltorch", "-ltorch_cpu", "-lc10", "-lc10_cuda", "-ltorch_cuda"]
+    return cflags, libs
+
+
+def compile_torch_objects():
+    """Compiles the two LibTorch translation units (the slow part) in parallel."""
+    cflags, _ = _torch_flags()
+    src_dir = os.path.join(CSRC, "torch")
+    hdr = os.path.join(ROOT, "include", "noa_gb300", "dcs_cuda.hh")
+    os.makedirs(BUILD, exist_ok=True)
+    jobs = []
+    for name, extra in (("dcs_cuda", []),
+                        ("muons_cuda", ["-DTORCH_EXTENSION_NAME=_muons_cuda", "-DTORCH_API_INCLUDE_EXTENSION_H"])):
+        src = os.path.join(src_dir, name + ".cpp")
+        obj = os.path.join(BUILD, name + ".torch.o")
+        if _stale(obj, [src, hdr, os.path.join(ROOT, "include", "noa_dcs.h")]):
+            jobs.append(["g++"] + cflags + extra + ["-c", src, "-o", obj])
+    with cf.ThreadPoolExecutor(max_workers=2) as ex:
+        list(ex.map(_run, jobs))
+    return [os.path.join(BUILD, n + ".torch.o") for n in ("dcs_cuda", "muons_cuda")]
+
+
+def build_torch(objs=None):
+    """LibTorch drop-in (libnoa_dcs_torch.so, the noa::pms::dcs::cuda symbols)
+    and the Python module _muons_cuda that mirrors the reference notebook's
+    muons_cuda extension.  Needs libnoa_dcs.so built first."""
+    import sysconfig
+    _, libs = _torch_flags()
+    o_dropin, o_mod = objs or compile_torch_objects()
+    if _stale(TORCH_LIB, [o_dropin, LIB]):
+        _run(["g++", "-shared", o_dropin, "-o", TORCH_LIB, "-L", PKG, "-lnoa_dcs"] + libs)
+    ext = os.path.join(PKG, "_muons_cuda" + sysconfig.get_config_var("EXT_SUFFIX"))
+    if _stale(ext, [o_mod, TORCH_LIB]):
+        _run(["g++", "-shared", o_mod, "-o", ext, "-L", PKG, "-lnoa_dcs_torch", "-lnoa_dcs"] + libs +
+             ["-ltorch_python"])
+    return TORCH_LIB, ext
+
+
 def build_oracle():
     src = os.path.join(ORACLE_DIR, "dcs_oracle.cpp")
     hdr = os.path.join(ORACLE_DIR, "dcs_oracle.hpp")
@@ -97,13 +151,16 @@ def build_ref(noa_checkout="/root/reference"):
     return REF_LIB
 
 
-def build_all(ref=True, verbose=False):
-    with cf.ThreadPoolExecutor(max_workers=3) as ex:
+def build_all(ref=True, torch_layer=True, verbose=False):
+    with cf.ThreadPoolExecutor(max_workers=4) as ex:
         f_cuda = ex.submit(build_cuda, verbose)
         f_oracle = ex.submit(build_oracle)
         f_ref = ex.submit(build_ref) if ref else None
+        f_tobj = ex.submit(compile_torch_objects) if torch_layer else None
         out = {"cuda": f_cuda.result(), "oracle": f_oracle.result()}
         out["ref"] = f_ref.result() if f_ref else None
+        if torch_layer:
+            out["torch"] = build_torch(f_tobj.result())
     return out
 
 

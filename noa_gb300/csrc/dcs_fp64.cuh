@@ -13,7 +13,10 @@
  *
  * The `*_live` predicates evaluate only the kinematic bounds of a process
  * (the reference's early returns) so that a kernel can drop the pairs whose
- * DCS is exactly zero before running the quadrature.
+ * DCS is exactly zero before running the quadrature.  Bound expressions use
+ * the __d*_rn intrinsics, which the compiler never fuses into an FMA, so the
+ * zero / non-zero decision rounds exactly as the reference's (unfused) CPU
+ * code does, also for pairs placed exactly on a bound.
  */
 #pragma once
 
@@ -68,7 +71,7 @@ __device__ __forceinline__ double pprod_argmin(double K, double q, const noa_dcs
     const double gamma = 1. + K / c.mass;
     const double x0 = 4. * ME / q;
     const double x1 = 6. / (gamma * (gamma - q / c.mass));
-    return (x0 + 2. * (1. - x0) * x1) / (1. + (1. - x1) * sqrt(1. - x0));
+    return __dadd_rn(x0, __dmul_rn(2. * (1. - x0), x1)) / __dadd_rn(1., __dmul_rn(1. - x1, sqrt(1. - x0)));
 }
 
 __device__ __forceinline__ bool pprod_live(double K, double q, const noa_dcs_consts &c) {
@@ -92,9 +95,7 @@ __device__ __forceinline__ double pprod_fp64(double K, double q, const noa_dcs_c
     const double beta = 0.5 * nu * nu / (1. - nu);
     const double xi_factor = c.pp_half_r2 * beta;
     const double gamma = 1. + K / mass;
-    const double x0 = 4. * ME / q;
-    const double x1 = 6. / (gamma * (gamma - q / mass));
-    const double argmin = (x0 + 2. * (1. - x0) * x1) / (1. + (1. - x1) * sqrt(1. - x0));
+    const double argmin = pprod_argmin(K, q, c);
     if ((argmin >= 1.) || (argmin <= 0.))
         return 0.;
     const double tmin = log(argmin);
@@ -198,7 +199,7 @@ __device__ __forceinline__ bool photo_live(double K, double q, const noa_dcs_con
         return false;
     const double y = q / E;
     const double Q2min = mass * mass * y * y / (1 - y);
-    const double Q2max = 2.0 * PH_M * (q - PH_MPI) - PH_MPI * PH_MPI;
+    const double Q2max = __dsub_rn(__dmul_rn(2.0 * PH_M, q - PH_MPI), PH_MPI * PH_MPI);
     if ((Q2max < Q2min) | (Q2min < 0))
         return false;
     return true;
@@ -213,7 +214,7 @@ __device__ __forceinline__ double photo_fp64(double K, double q, const noa_dcs_c
         return 0.;
     const double y = q / E;
     const double Q2min = mass * mass * y * y / (1 - y);
-    const double Q2max = 2.0 * PH_M * (q - PH_MPI) - PH_MPI * PH_MPI;
+    const double Q2max = __dsub_rn(__dmul_rn(2.0 * PH_M, q - PH_MPI), PH_MPI * PH_MPI);
     if ((Q2max < Q2min) | (Q2min < 0))
         return 0.;
     const double pQ2min = log(Q2min);
@@ -259,7 +260,7 @@ __device__ __forceinline__ double ion_fp64(double K, double q, const noa_dcs_con
     const double mass = c.mass;
     const double P2 = K * (K + 2. * mass);
     const double E = K + mass;
-    const double Wmax = 2. * ME * P2 / (mass * mass + ME * (ME + 2. * E));
+    const double Wmax = 2. * ME * P2 / __dadd_rn(__dmul_rn(mass, mass), __dmul_rn(ME, ME + 2. * E));
     if ((Wmax < NOA_X_FRACTION * K) || (q > Wmax))
         return 0.;
     if (q <= c.io_Wmin)
