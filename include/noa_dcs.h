@@ -114,6 +114,12 @@ int noa_dcs_abi_version(void);
  * FP64 / FP32 pipe peaks that the DCS kernels' rooflines are quoted against. */
 int noa_dcs_probe_fma(int fp64, void *out, int blocks, int iters, double *flops, void *stream);
 
+/* Diagnostics (no counterpart in the reference): out[i] = f(x[i]) (or
+ * f(x[i], y[i])) for one of the library's FP64 elementary functions --
+ * fn 0 log, 1 exp, 2 reciprocal, 3 division x/y, 4 sqrt -- on device buffers,
+ * so that their error can be measured against a reference libm. */
+int noa_dcs_lean64_eval(int fn, const double *x, const double *y, double *out, int64_t n, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -53,6 +53,7 @@ SIGNATURES = {
     "noa_dcs_last_error": (ctypes.c_char_p, []),
     "noa_dcs_abi_version": (_INT, []),
     "noa_dcs_probe_fma": (_INT, [_INT, _P, _INT, _INT, ctypes.POINTER(_D), _P]),
+    "noa_dcs_lean64_eval": (_INT, [_INT, _P, _P, _P, _I64, _P]),
 }
 
 _lib = None

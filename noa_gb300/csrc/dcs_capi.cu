@@ -135,6 +135,9 @@ void noa_dcs_fill_consts(noa_dcs_consts *c, double A, double I, int32_t Z, doubl
     c->mass = mass;
     c->Z = Z;
     c->Zd = (double)Z;
+    c->inv_mass = 1. / mass;
+    c->inv_m2 = 1. / (mass * mass);
+    c->scale_A = 1E+03 * NOA_AVOGADRO_NUMBER / A;
     { // physics.hh:121-133
         const double sqrte = 1.648721271;
         c->br_phie_factor = mass / (me * me * sqrte);
@@ -160,6 +163,7 @@ void noa_dcs_fill_consts(noa_dcs_consts *c, double A, double I, int32_t Z, doubl
         c->pp_cLe = 2.25 * Z13 * Z13 / (r * r);
         c->pp_half_r2 = 0.5 * r * r;
         c->pp_r2 = r * r;
+        c->pp_inv_r2 = 1. / (r * r);
         c->pp_r_AZ13 = r * c->pp_AZ13;
         c->pp_15_Z13 = 1.5 * Z13;
         c->pp_cZ = 1.794664E-34 * (double)Z;
@@ -172,11 +176,13 @@ void noa_dcs_fill_consts(noa_dcs_consts *c, double A, double I, int32_t Z, doubl
         c->ph_a_low = std::exp(-0.1 * std::log(A));
         c->ph_q_min = mpi * (1.0 + 0.5 * mpi / M);
         c->ph_log_q02 = std::log(0.52544 / 0.06527);
+        c->ph_inv_log_q02 = 1. / c->ph_log_q02;
     }
     { // dcs.hh:422, 435-436
         c->io_Wmin = 0.62 * I;
         const double m1 = mass - me;
         c->io_k_rad = 0.5 * m1 * m1 / me;
+        c->io_cZA = 1.535336E-05 * (double)Z / A;
     }
 }
 

@@ -34,6 +34,9 @@ typedef struct noa_dcs_consts {
     double Zd;      /* (double) Z */
     int32_t Z;
     int32_t pad_;
+    double inv_mass;        /* 1 / mass */
+    double inv_m2;          /* 1 / (mass mass) */
+    double scale_A;         /* 1e3 N_A / A: the macroscopic factor of every process */
 
     /* bremsstrahlung, physics.hh:119-133 */
     double br_phie_factor;  /* mass / (me me sqrte) */
@@ -54,6 +57,7 @@ typedef struct noa_dcs_consts {
     double pp_cLe;          /* 2.25 Z13 Z13 / (r r) */
     double pp_half_r2;      /* 0.5 r r */
     double pp_r2;           /* r r */
+    double pp_inv_r2;       /* 1 / (r r) */
     double pp_r_AZ13;       /* r AZ13 */
     double pp_15_Z13;       /* 1.5 Z13 */
     double pp_cZ;           /* 1.794664e-34 Z */
@@ -65,10 +69,12 @@ typedef struct noa_dcs_consts {
     double ph_a_low;        /* exp(-0.1 log A), x < 0.0014 branch */
     double ph_q_min;        /* mpi (1 + 0.5 mpi / M) */
     double ph_log_q02;      /* log(Q02 / Lambda2), ALLM */
+    double ph_inv_log_q02;  /* 1 / log(Q02 / Lambda2) */
 
     /* ionisation, dcs.hh:408-443 */
     double io_Wmin;         /* 0.62 I */
     double io_k_rad;        /* 0.5 m1 m1 / me, radiative-correction threshold */
+    double io_cZA;          /* 1.535336e-5 Z / A */
 } noa_dcs_consts;
 
 /* Fills c from (A, I, Z, mass) with the reference's expressions. */

@@ -1,28 +1,44 @@
 /*
  * FP64 device functions of the four muon DCS processes.
  *
- * Each function keeps the reference's operation order inside one evaluation;
- * what depends only on (element, mass) comes precomputed in noa_dcs_consts
- * (dcs_consts.h).  Every early exit of the reference is kept with the same
- * predicate, so NaN inputs propagate as they do on the CPU.
- *
  *   bremsstrahlung   physics.hh:114-153
  *   pair production  dcs.hh:144-258, 8-node GL numerics.hh:110-129
  *   photonuclear     dcs.hh:261-405, 9-node GL numerics.hh:131-152
  *   ionisation       dcs.hh:408-443
  *
- * The `*_live` predicates evaluate only the kinematic bounds of a process
- * (the reference's early returns) so that a kernel can drop the pairs whose
- * DCS is exactly zero before running the quadrature.  Bound expressions use
- * the __d*_rn intrinsics, which the compiler never fuses into an FMA, so the
- * zero / non-zero decision rounds exactly as the reference's (unfused) CPU
- * code does, also for pairs placed exactly on a bound.
+ * Accuracy contract: FP64 -- the reference's own metric (mean relative error,
+ * common.hh:228-236) against its CPU output stays below 1e-12.  The formulas
+ * are the reference's; what differs is how they are evaluated on a GPU whose
+ * FP64 pipe is ~70x slower than its FP32 pipe:
+ *
+ *  - what depends only on (element, mass) comes precomputed in
+ *    noa_dcs_consts (dcs_consts.h), bit-identical to the reference's values;
+ *  - log / exp / division / sqrt inside the quadrature bodies use the lean64
+ *    functions (lean64.cuh): same accuracy class, a third of the FP64
+ *    instructions; divisions by a shared denominator reuse one reciprocal;
+ *  - branch tests on non-negative doubles compare bit patterns on the
+ *    integer pipe (lean64::bits_ge).
+ *
+ * Every early exit of the reference is decided exactly as the reference
+ * decides it: the bound expressions are evaluated in IEEE arithmetic in the
+ * reference's order, with __d*_rn intrinsics where the compiler could
+ * otherwise fuse a product into an addition.  The zero / non-zero pattern is
+ * therefore identical, also for pairs placed exactly on a bound, and NaN
+ * inputs propagate as on the CPU.  The `*_live` predicates evaluate only those
+ * bounds, so that a kernel can drop closed pairs before the quadrature.
  */
 #pragma once
 
 #include "dcs_consts.h"
+#include "lean64.cuh"
 
 namespace noa_dcs {
+
+using lean64::bits_ge;
+using lean64::lean_div;
+using lean64::lean_exp;
+using lean64::lean_log;
+using lean64::lean_rcp;
 
 // Gauss-Legendre literals, numerics.hh:116-121 (8 nodes on [0,1]) and
 // numerics.hh:137-144 (9 nodes on [-1,1]).  They are the reference's 8-digit
@@ -41,37 +57,47 @@ __constant__ double kGL9W[9] = {0.3302393550012598, 0.1806481606948574, 0.180648
 constexpr double ME = NOA_ELECTRON_MASS;
 constexpr double NA = NOA_AVOGADRO_NUMBER;
 
+// Clamp of the reference's `if (v < 0.) v = 0.;` that keeps NaN.
+__device__ __forceinline__ double clamp0(double v) {
+    const long long b = __double_as_longlong(v);
+    return (b < 0 && (b & 0x7FFFFFFFFFFFFFFFLL) <= 0x7FF0000000000000LL) ? 0. : v;
+}
+
 // ---------------------------------------------------------------- bremsstrahlung
 __device__ __forceinline__ double brems_fp64(double K, double q, const noa_dcs_consts &c) {
     const double mass = c.mass;
     const double sqrte = 1.648721271;
     const double E = K + mass;
-    const double delta_factor = c.br_half_m2 / E;
-    const double qe_max = E / (1. + c.br_half_m2 / (ME * E));
-    const double nu = q / E;
-    const double delta = delta_factor * nu / (1. - nu);
-    double Phi_n = log(c.br_BZ_n * (mass + delta * c.br_Dn_sqrte_m2) / (c.br_D_n * (ME + delta * sqrte * c.br_BZ_n)));
-    if (Phi_n < 0.)
-        Phi_n = 0.;
-    double Phi_e;
-    if (q < qe_max) {
-        Phi_e = log(c.br_BZe_mass / ((1. + delta * c.br_phie_factor) * (ME + delta * sqrte * c.br_BZ_e)));
-        if (Phi_e < 0.)
-            Phi_e = 0.;
-    } else
-        Phi_e = 0.;
-    const double dcs = c.br_dcs_factor * (c.Zd * Phi_n + Phi_e) * (4. / 3. * (1. / nu - 1.) + nu);
-    return (dcs < 0.) ? 0. : dcs * 1E+03 * NA / c.A;
+    const double invE = lean_rcp(E);
+    const double delta_factor = c.br_half_m2 * invE;
+    // q < qe_max decides whether the electron term exists (physics.hh:142);
+    // decided in IEEE arithmetic like the reference when q is within 64 ulp.
+    const double qe_lean = E * lean_rcp(1. + c.br_half_m2 * lean_rcp(ME * E));
+    bool below = q < qe_lean;
+    const long long dist = __double_as_longlong(q) - __double_as_longlong(qe_lean);
+    if (dist < 64 && dist > -64)
+        below = q < __ddiv_rn(E, __dadd_rn(1., __ddiv_rn(c.br_half_m2, __dmul_rn(ME, E))));
+    const double nu = __ddiv_rn(q, E);  // as the reference: 1 - nu cancels as q -> E
+    const double delta = delta_factor * nu * lean_rcp(1. - nu);
+    const double Phi_n = clamp0(lean_log(c.br_BZ_n * (mass + delta * c.br_Dn_sqrte_m2) *
+                                         lean_rcp(c.br_D_n * (ME + delta * sqrte * c.br_BZ_n))));
+    double Phi_e = 0.;
+    if (below)
+        Phi_e = clamp0(lean_log(c.br_BZe_mass *
+                                lean_rcp((1. + delta * c.br_phie_factor) * (ME + delta * sqrte * c.br_BZ_e))));
+    const double dcs = c.br_dcs_factor * (c.Zd * Phi_n + Phi_e) * (4. / 3. * (lean_rcp(nu) - 1.) + nu);
+    return (dcs < 0.) ? 0. : dcs * c.scale_A;
 }
 
 // ---------------------------------------------------------------- pair production
-// Lower end of the t-integral, argmin of dcs.hh:169-173; returns a value
-// outside (0, 1) when the pair is kinematically closed.
-__device__ __forceinline__ double pprod_argmin(double K, double q, const noa_dcs_consts &c) {
-    const double gamma = 1. + K / c.mass;
-    const double x0 = 4. * ME / q;
-    const double x1 = 6. / (gamma * (gamma - q / c.mass));
-    return __dadd_rn(x0, __dmul_rn(2. * (1. - x0), x1)) / __dadd_rn(1., __dmul_rn(1. - x1, sqrt(1. - x0)));
+// Lower end of the t-integral, argmin of dcs.hh:169-173, in the reference's
+// IEEE arithmetic (its rounding decides both the bound and tmin near 1).
+__device__ __forceinline__ double pprod_argmin_exact(double K, double q, const noa_dcs_consts &c) {
+    const double gamma = __dadd_rn(1., __ddiv_rn(K, c.mass));
+    const double x0 = __ddiv_rn(4. * ME, q);
+    const double x1 = __ddiv_rn(6., __dmul_rn(gamma, __dsub_rn(gamma, __ddiv_rn(q, c.mass))));
+    return __ddiv_rn(__dadd_rn(x0, __dmul_rn(__dmul_rn(2., __dsub_rn(1., x0)), x1)),
+                     __dadd_rn(1., __dmul_rn(__dsub_rn(1., x1), __dsqrt_rn(__dsub_rn(1., x0)))));
 }
 
 __device__ __forceinline__ bool pprod_live(double K, double q, const noa_dcs_consts &c) {
@@ -79,10 +105,17 @@ __device__ __forceinline__ bool pprod_live(double K, double q, const noa_dcs_con
         return false;
     if (q >= K + c.pp_kmax_shift)
         return false;
-    const double argmin = pprod_argmin(K, q, c);
-    if ((argmin >= 1.) || (argmin <= 0.))
-        return false;
-    return true;
+    // cheap estimate of argmin; exact only where the decision is close
+    const double gamma = 1. + K * c.inv_mass;
+    const double x0 = 4. * ME * lean_rcp(q);
+    const double x1 = 6. * lean_rcp(gamma * (gamma - q * c.inv_mass));
+    const double a = (x0 + 2. * (1. - x0) * x1) * lean_rcp(1. + (1. - x1) * lean64::lean_sqrt(1. - x0));
+    const long long d1 = __double_as_longlong(a) - __double_as_longlong(1.0);
+    if ((d1 < 256 && d1 > -256) || !(fabs(a) > 1e-12)) {
+        const double am = pprod_argmin_exact(K, q, c);
+        return !((am >= 1.) || (am <= 0.));
+    }
+    return !((a >= 1.) || (a <= 0.));
 }
 
 __device__ __forceinline__ double pprod_fp64(double K, double q, const noa_dcs_consts &c) {
@@ -90,80 +123,115 @@ __device__ __forceinline__ double pprod_fp64(double K, double q, const noa_dcs_c
         return 0.;
     if (q >= K + c.pp_kmax_shift)
         return 0.;
-    const double mass = c.mass;
-    const double nu = q / (K + mass);
-    const double beta = 0.5 * nu * nu / (1. - nu);
-    const double xi_factor = c.pp_half_r2 * beta;
-    const double gamma = 1. + K / mass;
-    const double argmin = pprod_argmin(K, q, c);
+    const double argmin = pprod_argmin_exact(K, q, c);
     if ((argmin >= 1.) || (argmin <= 0.))
         return 0.;
-    const double tmin = log(argmin);
+    const double mass = c.mass;
+    const double E = K + mass;
+    const double nu = __ddiv_rn(q, E);
+    const double beta = 0.5 * nu * nu * lean_rcp(1. - nu);
+    const double xi_factor = c.pp_half_r2 * beta;
+    const double tmin = lean_log(argmin);
+    // Le's two logs share one: log(AZ13 sqrt(xe) q / D1) - log(D2)/2 = log(AZ13^2 q^2 xe / (D1^2 D2)) / 2
+    const double aq2 = (c.pp_AZ13 * q) * (c.pp_AZ13 * q);
+    const double b2 = 2. * beta, b15 = 1.5 * beta, b3 = 3. * beta, b4 = 4. * beta;
 
     double I = 0.;
 #pragma unroll
     for (int j = 0; j < 8; j++) {
-        const double eps = exp(kGL8X[j] * tmin);
+        const double eps = lean_exp(kGL8X[j] * tmin);
         const double rho = 1. - eps;
         const double rho2 = rho * rho;
         const double rho21 = eps * (2. - eps);
         const double xi = xi_factor * rho21;
-        const double xi_i = 1. / xi;
+        const double xi_i = lean_rcp(xi);
+        const double opxi = 1. + xi;
+        const double inv_opxi = lean_rcp(opxi);
 
         double Be;
-        if (xi >= 1E+03)
-            Be = 0.5 * xi_i * ((3. - rho2) + 2. * beta * (1. + rho2));
+        if (bits_ge(xi, 1E+03))
+            Be = 0.5 * xi_i * ((3. - rho2) + b2 * (1. + rho2));
         else
-            Be = ((2. + rho2) * (1. + beta) + xi * (3. + rho2)) * log(1. + xi_i) + (rho21 - beta) / (1. + xi) - 3. -
-                 rho2;
-        const double Ye = (5. - rho2 + 4. * beta * (1. + rho2)) /
-                          (2. * (1. + 3. * beta) * log(3. + xi_i) - rho2 - 2. * beta * (2. - rho2));
-        const double xe = (1. + xi) * (1. + Ye);
-        const double cLi = c.pp_cL / rho21;
-        const double Le = log(c.pp_AZ13 * sqrt(xe) * q / (q + cLi * xe)) - 0.5 * log(1. + c.pp_cLe * xe);
-        double Phi_e = Be * Le;
-        if (Phi_e < 0.)
-            Phi_e = 0.;
+            Be = ((2. + rho2) * (1. + beta) + xi * (3. + rho2)) * lean_log(1. + xi_i) + (rho21 - beta) * inv_opxi -
+                 3. - rho2;
+        const double Ye = lean_div(5. - rho2 + b4 * (1. + rho2),
+                                   2. * (1. + b3) * lean_log(3. + xi_i) - rho2 - b2 * (2. - rho2));
+        const double xe = opxi * (1. + Ye);
+        const double cLi = c.pp_cL * lean_rcp(rho21);
+        const double d1 = q + cLi * xe;
+        const double Le = 0.5 * lean_log(aq2 * xe * lean_rcp(d1 * d1 * (1. + c.pp_cLe * xe)));
+        const double Phi_e = clamp0(Be * Le);
 
         double Bmu;
-        if (xi <= 1E-03)
+        if (!bits_ge(xi, 1.0000000000000002E-03))  // xi <= 1e-3
             Bmu = 0.5 * xi * (5. - rho2 + beta * (3. + rho2));
         else
-            Bmu = ((1. + rho2) * (1. + 1.5 * beta) - xi_i * (1. + 2. * beta) * rho21) * log(1. + xi) +
-                  xi * (rho21 - beta) / (1. + xi) + (1. + 2. * beta) * rho21;
-        const double Ymu = (4. + rho2 + 3. * beta * (1. + rho2)) /
-                           ((1. + rho2) * (1.5 + 2. * beta) * log(3. + xi) + 1. - 1.5 * rho2);
-        const double xmu = (1. + xi) * (1. + Ymu);
-        const double Lmu = log(c.pp_r_AZ13 * q / (c.pp_15_Z13 * (q + cLi * xmu)));
-        double Phi_mu = Bmu * Lmu;
-        if (Phi_mu < 0.)
-            Phi_mu = 0.;
-        const double f = -(Phi_e + Phi_mu / c.pp_r2) * (1. - rho) * tmin;
-        I += f * kGL8W[j];
+            Bmu = ((1. + rho2) * (1. + b15) - xi_i * (1. + b2) * rho21) * lean_log(opxi) +
+                  xi * (rho21 - beta) * inv_opxi + (1. + b2) * rho21;
+        const double Ymu = lean_div(4. + rho2 + b3 * (1. + rho2),
+                                    (1. + rho2) * (1.5 + b2) * lean_log(3. + xi) + 1. - 1.5 * rho2);
+        const double xmu = opxi * (1. + Ymu);
+        const double Lmu = lean_log(c.pp_r_AZ13 * q * lean_rcp(c.pp_15_Z13 * (q + cLi * xmu)));
+        const double Phi_mu = clamp0(Bmu * Lmu);
+        const double f = -(Phi_e + Phi_mu * c.pp_inv_r2) * (1. - rho) * tmin;
+        I = fma(f, kGL8W[j], I);
     }
 
-    double zeta;
-    if (gamma <= 35.)
-        zeta = 0.;
-    else {
-        zeta = 0.073 * log(gamma / (1. + c.pp_gamma1 * gamma * c.pp_Z13 * c.pp_Z13)) - 0.26;
+    const double gamma = __dadd_rn(1., __ddiv_rn(K, mass));
+    double zeta = 0.;
+    if (!(gamma <= 35.)) {
+        zeta = 0.073 * lean_log(gamma * lean_rcp(1. + c.pp_gamma1 * gamma * c.pp_Z13 * c.pp_Z13)) - 0.26;
         if (zeta <= 0.)
             zeta = 0.;
         else
-            zeta /= 0.058 * log(gamma / (1. + c.pp_gamma2 * gamma * c.pp_Z13)) - 0.14;
+            zeta = lean_div(zeta, 0.058 * lean_log(gamma * lean_rcp(1. + c.pp_gamma2 * gamma * c.pp_Z13)) - 0.14);
     }
-    const double E = K + mass;
-    const double dcs = c.pp_cZ * (c.Zd + zeta) * (E - q) * I / (q * E);
-    return (dcs < 0.) ? 0. : dcs * 1E+03 * NA * (mass + K) / c.A;
+    const double dcs = lean_div(c.pp_cZ * (c.Zd + zeta) * (E - q) * I, q * E);
+    return (dcs < 0.) ? 0. : dcs * (mass + K) * c.scale_A;
 }
 
 // ---------------------------------------------------------------- photonuclear
 constexpr double PH_M = 0.931494;
 constexpr double PH_MPI = 0.134977;
 
-// ALLM F2, dcs.hh:261-307.
-__device__ __forceinline__ double ph_f2_allm(double x, double Q2, double log_q02) {
-    const double m02 = 0.31985, mP2 = 49.457, mR2 = 0.15052, Q02 = 0.52544, Lambda2 = 0.06527;
+// Photonuclear kinematic window, dcs.hh:357-381, in the reference's IEEE
+// arithmetic.  Returns false when the reference returns 0 before its
+// quadrature; on true, Q2min / Q2max are the reference's values.
+__device__ __forceinline__ bool photo_window(double K, double q, const noa_dcs_consts &c, double &Q2min,
+                                             double &Q2max) {
+    if ((q < 1.) || (q < 2E-03 * K))
+        return false;
+    const double mass = c.mass;
+    const double E = K + mass;
+    if ((q >= (E - mass)) || (q <= c.ph_q_min))
+        return false;
+    const double y = __ddiv_rn(q, E);
+    Q2min = __ddiv_rn(__dmul_rn(__dmul_rn(__dmul_rn(mass, mass), y), y), __dsub_rn(1., y));
+    Q2max = __dsub_rn(__dmul_rn(2.0 * PH_M, q - PH_MPI), PH_MPI * PH_MPI);
+    if ((Q2max < Q2min) | (Q2min < 0))
+        return false;
+    return true;
+}
+
+__device__ __forceinline__ bool photo_live(double K, double q, const noa_dcs_consts &c) {
+    double a, b;
+    return photo_window(K, q, c, a, b);
+}
+
+__device__ __forceinline__ double photo_fp64(double K, double q, const noa_dcs_consts &c) {
+    double Q2min, Q2max;
+    if (!photo_window(K, q, c, Q2min, Q2max))
+        return 0.;
+    const double mass = c.mass;
+    const double E = K + mass;
+    const double y = __ddiv_rn(q, E);
+    const double pQ2min = lean_log(Q2min);
+    const double pQ2max = lean_log(Q2max);
+    const double dpQ2 = pQ2max - pQ2min;
+    const double pQ2c = 0.5 * (pQ2max + pQ2min);
+
+    // ALLM parameters, dcs.hh:262-288.
+    const double m02 = 0.31985, mP2 = 49.457, mR2 = 0.15052, Q02 = 0.52544;
     const double cP1 = 0.28067, cP2 = 0.22291, cP3 = 2.1979;
     const double aP1 = -0.0808, aP2 = -0.44812, aP3 = 1.1709;
     const double bP1 = 0.36292, bP2 = 1.8917, bP3 = 1.8439;
@@ -171,88 +239,61 @@ __device__ __forceinline__ double ph_f2_allm(double x, double Q2, double log_q02
     const double aR1 = 0.58400, aR2 = 0.37888, aR3 = 2.6063;
     const double bR1 = 0.01147, bR2 = 3.7582, bR3 = 0.49338;
     const double M2 = 0.8803505929;
-    const double W2 = M2 + Q2 * (1.0 / x - 1.0);
-    const double t = log(log((Q2 + Q02) / Lambda2) / log_q02);
-    const double xP = (Q2 + mP2) / (Q2 + mP2 + W2 - M2);
-    const double xR = (Q2 + mR2) / (Q2 + mR2 + W2 - M2);
-    const double lnt = log(t);
-    const double cP = cP1 + (cP1 - cP2) * (1.0 / (1.0 + exp(cP3 * lnt)) - 1.0);
-    const double aP = aP1 + (aP1 - aP2) * (1.0 / (1.0 + exp(aP3 * lnt)) - 1.0);
-    const double bP = bP1 + bP2 * exp(bP3 * lnt);
-    const double cR = cR1 + cR2 * exp(cR3 * lnt);
-    const double aR = aR1 + aR2 * exp(aR3 * lnt);
-    const double bR = bR1 + bR2 * exp(bR3 * lnt);
-    const double l1x = log(1 - x);
-    const double F2P = cP * exp(aP * log(xP) + bP * l1x);
-    const double F2R = cR * exp(aR * log(xR) + bR * l1x);
-    return Q2 / (Q2 + m02) * (F2P + F2R);
-}
+    const double inv_lambda2 = 1. / 0.06527;
+    const double inv_ln10 = 0.43429448190325182765;
 
-// Photonuclear DCS kinematic window, dcs.hh:357-381.  Returns false when the
-// reference returns 0 before its quadrature.
-__device__ __forceinline__ bool photo_live(double K, double q, const noa_dcs_consts &c) {
-    if ((q < 1.) || (q < 2E-03 * K))
-        return false;
-    const double mass = c.mass;
-    const double E = K + mass;
-    if ((q >= (E - mass)) || (q <= c.ph_q_min))
-        return false;
-    const double y = q / E;
-    const double Q2min = mass * mass * y * y / (1 - y);
-    const double Q2max = __dsub_rn(__dmul_rn(2.0 * PH_M, q - PH_MPI), PH_MPI * PH_MPI);
-    if ((Q2max < Q2min) | (Q2min < 0))
-        return false;
-    return true;
-}
-
-__device__ __forceinline__ double photo_fp64(double K, double q, const noa_dcs_consts &c) {
-    if ((q < 1.) || (q < 2E-03 * K))
-        return 0.;
-    const double mass = c.mass;
-    const double E = K + mass;
-    if ((q >= (E - mass)) || (q <= c.ph_q_min))
-        return 0.;
-    const double y = q / E;
-    const double Q2min = mass * mass * y * y / (1 - y);
-    const double Q2max = __dsub_rn(__dmul_rn(2.0 * PH_M, q - PH_MPI), PH_MPI * PH_MPI);
-    if ((Q2max < Q2min) | (Q2min < 0))
-        return 0.;
-    const double pQ2min = log(Q2min);
-    const double pQ2max = log(Q2max);
-    const double dpQ2 = pQ2max - pQ2min;
-    const double pQ2c = 0.5 * (pQ2max + pQ2min);
-
-    // d2sigma/dQ2 pieces that do not depend on Q2, dcs.hh:338-343.
     const double cf = 2.603096E-35;
-    const double EE = E * E;
+    const double invEE = lean_rcp(E * E);
+    const double inv_q = lean_rcp(q);
     const double Mq = PH_M * q;
+    const double inv_Mq = lean_rcp(Mq);
+    const double two_Mq = 2. * Mq;
     const double two_m2 = 2 * mass * mass;
+    const double yy = y * y;
     double ds = 0.;
 #pragma unroll 1
     for (int j = 0; j < 9; j++) {
-        const double Q2 = exp(pQ2c + 0.5 * dpQ2 * kGL9X[j]);
-        const double x = 0.5 * Q2 / Mq;
-        const double F2p = ph_f2_allm(x, Q2, c.ph_log_q02);
-        // DRSS shadowing, dcs.hh:310-319.
+        const double Q2 = lean_exp(pQ2c + 0.5 * dpQ2 * kGL9X[j]);
+        const double invQ2 = lean_rcp(Q2);
+        const double x = 0.5 * Q2 * inv_Mq;
+        // ALLM F2, dcs.hh:289-306
+        const double W2 = M2 + Q2 * (two_Mq * invQ2 - 1.0);
+        const double t = lean_log(lean_log((Q2 + Q02) * inv_lambda2) * c.ph_inv_log_q02);
+        const double xP = (Q2 + mP2) * lean_rcp(Q2 + mP2 + W2 - M2);
+        const double xR = (Q2 + mR2) * lean_rcp(Q2 + mR2 + W2 - M2);
+        const double lnt = lean_log(t);
+        const double cP = cP1 + (cP1 - cP2) * (lean_rcp(1.0 + lean_exp(cP3 * lnt)) - 1.0);
+        const double aP = aP1 + (aP1 - aP2) * (lean_rcp(1.0 + lean_exp(aP3 * lnt)) - 1.0);
+        const double bP = bP1 + bP2 * lean_exp(bP3 * lnt);
+        const double cR = cR1 + cR2 * lean_exp(cR3 * lnt);
+        const double aR = aR1 + aR2 * lean_exp(aR3 * lnt);
+        const double bR = bR1 + bR2 * lean_exp(bR3 * lnt);
+        const double l1x = lean_log(1 - x);
+        const double F2P = cP * lean_exp(aP * lean_log(xP) + bP * l1x);
+        const double F2R = cR * lean_exp(aR * lean_log(xR) + bR * l1x);
+        const double F2p = Q2 * lean_rcp(Q2 + m02) * (F2P + F2R);
+        // DRSS shadowing, dcs.hh:310-319
         double a = 1.0;
         if (x < 0.0014)
             a = c.ph_a_low;
         else if (x < 0.04)
-            a = exp((0.069 * log10(x) + 0.097) * c.ph_logA);
-        const double F2A = (0.5 * c.A * a * (2.0 + x * (-1.85 + x * (2.45 + x * (-2.35 + x)))) * F2p);
-        // Whitlow R, dcs.hh:322-332.
-        double q2 = Q2;
-        if (Q2 < 0.3)
-            q2 = 0.3;
-        const double theta = 1 + 12.0 * q2 / (1.0 + q2) * 0.015625 / (0.015625 + x * x);
-        const double R = (0.635 / log(q2 / 0.04) * theta + 0.5747 / q2 - 0.3534 / (0.09 + q2 * q2));
-        // dcs.hh:348-354.
-        const double dds = (1 - y + 0.5 * (1 - two_m2 / Q2) * (y * y + Q2 / EE) / (1 + R)) / (Q2 * Q2) -
-                           0.25 / (EE * Q2);
-        const double d2 = cf * F2A * dds / q;
-        ds += d2 * Q2 * kGL9W[j];
+            a = lean_exp((0.069 * (lean_log(x) * inv_ln10) + 0.097) * c.ph_logA);
+        const double F2A = 0.5 * c.A * a * (2.0 + x * (-1.85 + x * (2.45 + x * (-2.35 + x)))) * F2p;
+        // Whitlow R, dcs.hh:322-332
+        const bool low = !bits_ge(Q2, 0.3);
+        const double q2 = low ? 0.3 : Q2;
+        const double inv_q2 = low ? 1. / 0.3 : invQ2;
+        const double theta = 1 + 12.0 * q2 * 0.015625 * lean_rcp((1.0 + q2) * (0.015625 + x * x));
+        const double R = 0.635 * theta * lean_rcp(lean_log(q2 * 25.)) + 0.5747 * inv_q2 -
+                         0.3534 * lean_rcp(0.09 + q2 * q2);
+        // dcs.hh:348-354
+        const double dds = (1 - y + 0.5 * (1 - two_m2 * invQ2) * (yy + Q2 * invEE) * lean_rcp(1 + R)) *
+                               (invQ2 * invQ2) -
+                           0.25 * invEE * invQ2;
+        const double d2 = cf * F2A * dds * inv_q;
+        ds = fma(d2 * Q2, kGL9W[j], ds);
     }
-    return (ds < 0.) ? 0. : 0.5 * ds * dpQ2 * 1E+03 * NA * (mass + K) / c.A;
+    return (ds < 0.) ? 0. : 0.5 * ds * dpQ2 * (mass + K) * c.scale_A;
 }
 
 // ---------------------------------------------------------------- ionisation
@@ -260,19 +301,21 @@ __device__ __forceinline__ double ion_fp64(double K, double q, const noa_dcs_con
     const double mass = c.mass;
     const double P2 = K * (K + 2. * mass);
     const double E = K + mass;
-    const double Wmax = 2. * ME * P2 / __dadd_rn(__dmul_rn(mass, mass), __dmul_rn(ME, ME + 2. * E));
+    const double Wmax = __ddiv_rn(2. * ME * P2, __dadd_rn(__dmul_rn(mass, mass), __dmul_rn(ME, ME + 2. * E)));
     if ((Wmax < NOA_X_FRACTION * K) || (q > Wmax))
         return 0.;
     if (q <= c.io_Wmin)
         return 0.;
-    const double a0 = 0.5 / P2;
-    const double a1 = -1. / Wmax;
-    const double a2 = E * E / P2;
-    const double cs = 1.535336E-05 * E * c.Zd / c.A * (a0 + 1. / q * (a1 + a2 / q));
+    const double inv_P2 = lean_rcp(P2);
+    const double inv_q = lean_rcp(q);
+    const double a0 = 0.5 * inv_P2;
+    const double a1 = -lean_rcp(Wmax);
+    const double a2 = E * E * inv_P2;
+    const double cs = c.io_cZA * E * (a0 + inv_q * (a1 + a2 * inv_q));
     double Delta = 0.;
     if (K >= c.io_k_rad) {
-        const double L1 = log(1. + 2. * q / ME);
-        Delta = 1.16141E-03 * L1 * (log(4. * E * (E - q) / (mass * mass)) - L1);
+        const double L1 = lean_log(1. + q * (2. / ME));
+        Delta = 1.16141E-03 * L1 * (lean_log(4. * E * (E - q) * c.inv_m2) - L1);
     }
     return cs * (1. + Delta);
 }

@@ -1,0 +1,37 @@
+/*
+ * Diagnostics entry point: evaluates one lean64 function (lean64.cuh)
+ * element-wise so that tests can bound its error against a host libm.  No
+ * counterpart in the reference.
+ */
+#include "dcs_launch.h"
+#include "lean64.cuh"
+
+namespace {
+
+__global__ void lean64_eval_kernel(int fn, const double *__restrict__ x, const double *__restrict__ y, double *out,
+                                   int64_t n) {
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const double a = x[i];
+        double r;
+        switch (fn) {
+        case 0: r = lean64::lean_log(a); break;
+        case 1: r = lean64::lean_exp(a); break;
+        case 2: r = lean64::lean_rcp(a); break;
+        case 3: r = lean64::lean_div(a, y[i]); break;
+        default: r = lean64::lean_sqrt(a); break;
+        }
+        out[i] = r;
+    }
+}
+
+} // namespace
+
+extern "C" int noa_dcs_lean64_eval(int fn, const double *x, const double *y, double *out, int64_t n, void *stream) {
+    if (fn < 0 || fn > 4 || n < 0 || (n > 0 && (!x || !out || (fn == 3 && !y))))
+        return NOA_DCS_ERROR_INVALID_VALUE;
+    if (n == 0)
+        return NOA_DCS_SUCCESS;
+    const int64_t blocks = (n + 255) / 256;
+    lean64_eval_kernel<<<(int)(blocks < 4096 ? blocks : 4096), 256, 0, (cudaStream_t)stream>>>(fn, x, y, out, n);
+    return cudaGetLastError() == cudaSuccess ? NOA_DCS_SUCCESS : NOA_DCS_ERROR_CUDA;
+}

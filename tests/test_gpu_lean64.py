@@ -1,0 +1,75 @@
+"""Error bounds of the FP64 elementary functions in lean64.cuh, measured on
+the GPU against the host libm (numpy, correctly rounded or within 1 ulp)."""
+import numpy as np
+import pytest
+import torch
+
+from noa_gb300 import _lib
+
+pytestmark = pytest.mark.gpu
+
+
+def run(fn, x, y=None):
+    lib = _lib.load()
+    tx = torch.from_numpy(np.ascontiguousarray(x)).cuda()
+    ty = torch.from_numpy(np.ascontiguousarray(y)).cuda() if y is not None else tx
+    out = torch.empty_like(tx)
+    assert lib.noa_dcs_lean64_eval(fn, tx.data_ptr(), ty.data_ptr(), out.data_ptr(), tx.numel(), None) == 0
+    torch.cuda.synchronize()
+    return out.cpu().numpy()
+
+
+def ulps(got, exp):
+    """Error in units of the last place of the expected value."""
+    exp = np.asarray(exp, dtype=np.float64)
+    return np.abs(got - exp) / np.spacing(np.abs(exp))
+
+
+def sample(rng, n, lo, hi):
+    return np.exp(rng.uniform(np.log(lo), np.log(hi), n))
+
+
+def test_log(cuda_device):
+    rng = np.random.default_rng(1)
+    x = np.concatenate([sample(rng, 400000, 1e-300, 1e300), 1 + rng.uniform(-1e-2, 1e-2, 200000),
+                        1 + rng.uniform(-1e-9, 1e-9, 50000), [1.0, 2.0, 0.5, np.sqrt(2.0)]])
+    u = ulps(run(0, x), np.log(x))
+    assert u.max() <= 4.0, u.max()
+    assert u.mean() <= 0.5
+    special = np.array([0.0, -1.0, np.inf, np.nan, 5e-324, -0.0])
+    got = run(0, special)
+    with np.errstate(all="ignore"):
+        exp = np.log(special)
+    assert np.array_equal(np.isnan(got), np.isnan(exp)) and np.array_equal(got[~np.isnan(exp)],
+                                                                             exp[~np.isnan(exp)])
+
+
+def test_exp(cuda_device):
+    rng = np.random.default_rng(2)
+    x = np.concatenate([rng.uniform(-699, 699, 400000), rng.uniform(-1e-3, 1e-3, 100000),
+                        rng.uniform(-30, 30, 100000), [0.0, 1.0, -1.0]])
+    u = ulps(run(1, x), np.exp(x))
+    assert u.max() <= 4.0, u.max()
+    assert u.mean() <= 0.5
+    special = np.array([800.0, -800.0, np.inf, -np.inf, np.nan])
+    got = run(1, special)
+    with np.errstate(all="ignore"):
+        exp = np.exp(special)
+    assert np.array_equal(np.isnan(got), np.isnan(exp)) and np.array_equal(got[~np.isnan(exp)],
+                                                                             exp[~np.isnan(exp)])
+
+
+def test_reciprocal_division_sqrt(cuda_device):
+    rng = np.random.default_rng(3)
+    b = sample(rng, 300000, 1e-300, 1e300) * rng.choice([-1.0, 1.0], 300000)
+    a = sample(rng, 300000, 1e-100, 1e100)
+    assert ulps(run(2, b), 1.0 / b).max() <= 2.0
+    assert ulps(run(3, a, b), a / b).max() <= 3.0
+    x = sample(rng, 300000, 1e-300, 1e300)
+    assert ulps(run(4, x), np.sqrt(x)).max() <= 2.0
+    special = np.array([0.0, -0.0, np.inf, -np.inf, np.nan, 5e-324])
+    with np.errstate(all="ignore"):
+        for fn, ref in ((2, 1.0 / special), (4, np.sqrt(special))):
+            got = run(fn, special)
+            assert np.array_equal(np.isnan(got), np.isnan(ref))
+            assert np.array_equal(got[~np.isnan(ref)], ref[~np.isnan(ref)])
