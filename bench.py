@@ -209,6 +209,47 @@ def measure_fp64_peak(lib, torch, stream):
     return best
 
 
+def rel_error_stats(torch, got, ref):
+    """max / median relative error of got against ref over ref != 0, and
+    whether the zero patterns agree."""
+    nz = ref != 0
+    rel = ((got[nz] - ref[nz]).abs() / ref[nz].abs()).float()
+    return {"max_rel": float(rel.max()) if rel.numel() else 0.0,
+            "median_rel": float(rel.median()) if rel.numel() else 0.0,
+            "mean_rel": float(rel.mean()) if rel.numel() else 0.0,
+            "zero_pattern_equal": bool(torch.equal(got == 0, ref == 0))}
+
+
+def time_fp32c(lib, torch, tk, tq, ref_outs, n, el, mass, stream, args, fp64_s):
+    """FP32-compensated form (NOA_DCS_FP32C, tolerance 1e-6) on the same
+    pairs: evals/s per process, speed-up over the FP64 kernel, and its error
+    against the FP64 kernel's output."""
+    from noa_gb300 import _lib
+    out = torch.empty_like(tk)
+    res = {}
+    for p, name in enumerate(PROCESSES):
+        def launch():
+            _lib.check(lib.noa_dcs_cuda_vmap(p, 1, out.data_ptr(), tk.data_ptr(), tq.data_ptr(), n, el, mass,
+                                             stream.cuda_stream))
+        for _ in range(args.warmup):
+            launch()
+        s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        s.record(stream)
+        for _ in range(args.steps):
+            launch()
+        e.record(stream)
+        torch.cuda.synchronize()
+        t = s.elapsed_time(e) * 1e-3
+        res[name] = {"evals_per_s": n * args.steps / t, "ms_per_launch": 1e3 * t / args.steps,
+                     "speedup_vs_fp64": fp64_s[name] / t, "tolerance": 1e-6,
+                     **rel_error_stats(torch, out, ref_outs[p])}
+    total = sum(v["ms_per_launch"] for v in res.values())
+    res["all_processes"] = {"evals_per_s": 4 * n / (total * 1e-3),
+                            "speedup_vs_fp64": sum(fp64_s.values()) / args.steps / (total * 1e-3)}
+    return res
+
+
 def load_traffic():
     path = os.path.join(ROOT, "profiles", "traffic.json")
     try:
@@ -307,6 +348,9 @@ def run_ours(args):
             if not torch.equal(hout[p], outs[p].cpu()):
                 raise RuntimeError(f"e2e result differs from device result for {PROCESSES[p]}")
 
+    variants = {"fp64": {name: {"evals_per_s": n * args.steps / t} for name, t in per_proc_s.items()}}
+    variants["fp32c"] = time_fp32c(lib, torch, tk, tq, outs, n, el, MUON_MASS, stream, args, per_proc_s)
+
     if rank != 0:
         if world > 1:
             tdist.destroy_process_group()
@@ -333,6 +377,7 @@ def run_ours(args):
                      "peak_source": "FP64 FMA-chain probe (noa_dcs_probe_fma) measured in this run",
                      "numerator": f"{FLOP_EQ_PER_EVAL[dom]} flop-eq/eval x {n} evals per launch"},
         "per_process": per_process,
+        "variants": variants,
         "e2e": e2e,
         "clocks": clocks.summary(),
         "gpu_launches": 4 * args.steps,

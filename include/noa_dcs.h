@@ -47,8 +47,10 @@ typedef enum noa_dcs_process {
 
 /* Arithmetic of a launch.  FP64 is the drop-in: it matches the reference's
  * FP64 CPU path to a mean relative error below 1e-12.  FP32C runs the
- * quadrature bodies in FP32 with compensated node sums and keeps FP64 at the
- * kinematic edges; its error bound is stated per process by the tests. */
+ * quadrature bodies in FP32 with compensated node sums, keeps FP64 at the
+ * kinematic edges and bounds, and recomputes in FP64 every pair whose
+ * estimated relative error exceeds the tolerance (1e-6 by default), so its
+ * relative error against the FP64 result stays below that tolerance. */
 typedef enum noa_dcs_precision {
     NOA_DCS_FP64 = 0,
     NOA_DCS_FP32C = 1
@@ -83,6 +85,13 @@ int noa_dcs_cuda_vmap_ionisation(double *result, const double *K, const double *
  * (dcs.hh:35-48). */
 int noa_dcs_cuda_vmap(int process, int precision, double *result, const double *K, const double *q, int64_t n,
                       const noa_dcs_element *element, double mass, void *stream);
+
+/* FP32-compensated form with an explicit tolerance: every pair whose
+ * estimated relative error exceeds `tolerance` (0 < tolerance < 1) is
+ * recomputed in FP64.  noa_dcs_cuda_vmap with NOA_DCS_FP32C uses 1e-6.
+ * No counterpart in the reference (which has only FP64). */
+int noa_dcs_cuda_vmap_fp32c(int process, double *result, const double *K, const double *q, int64_t n,
+                            const noa_dcs_element *element, double mass, float tolerance, void *stream);
 
 /* Host-buffer form: K, q and result are HOST buffers (pinned memory gives
  * copy/compute overlap; pageable memory works but serialises the copies).

@@ -14,7 +14,9 @@
  */
 #pragma once
 
+#include <math.h>
 #include <stdint.h>
+#include <string.h>
 
 #ifdef __cplusplus
 extern "C" {
@@ -77,8 +79,66 @@ typedef struct noa_dcs_consts {
     double io_cZA;          /* 1.535336e-5 Z / A */
 } noa_dcs_consts;
 
-/* Fills c from (A, I, Z, mass) with the reference's expressions. */
-void noa_dcs_fill_consts(noa_dcs_consts *c, double A, double I, int32_t Z, double mass);
+/* Fills c from (A, I, Z, mass) with the reference's expressions (host code;
+ * compile with -ffp-contract=off). */
+static inline void noa_dcs_fill_consts(noa_dcs_consts *c, double A, double I, int32_t Z, double mass) {
+    memset(c, 0, sizeof *c);
+    const double me = NOA_ELECTRON_MASS;
+    c->A = A;
+    c->I = I;
+    c->mass = mass;
+    c->Z = Z;
+    c->Zd = (double)Z;
+    c->inv_mass = 1. / mass;
+    c->inv_m2 = 1. / (mass * mass);
+    c->scale_A = 1E+03 * NOA_AVOGADRO_NUMBER / A;
+    { // physics.hh:121-133
+        const double sqrte = 1.648721271;
+        c->br_phie_factor = mass / (me * me * sqrte);
+        const double rem = 5.63588E-13 * me / mass;
+        c->br_BZ_n = (Z == 1) ? 202.4 : 182.7 * pow((double)Z, -1. / 3.);
+        c->br_BZ_e = (Z == 1) ? 446. : 1429. * pow((double)Z, -2. / 3.);
+        c->br_D_n = 1.54 * pow(A, 0.27);
+        c->br_dcs_factor = 7.297182E-07 * rem * rem * (double)Z;
+        c->br_half_m2 = 0.5 * mass * mass;
+        c->br_Dn_sqrte_m2 = c->br_D_n * sqrte - 2.;
+        c->br_BZe_mass = c->br_BZ_e * mass;
+    }
+    { // dcs.hh:153-166, 235-241
+        const double sqrte = 1.6487212707;
+        const double Z13 = pow((double)Z, 1. / 3.);
+        c->pp_Z13 = Z13;
+        c->pp_kmax_shift = mass * (1. - 0.75 * sqrte * Z13);
+        const double r = mass / me;
+        c->pp_r = r;
+        const double A_ = (Z == 1) ? 202.4 : 183.;
+        c->pp_AZ13 = A_ / Z13;
+        c->pp_cL = 2. * sqrte * me * c->pp_AZ13;
+        c->pp_cLe = 2.25 * Z13 * Z13 / (r * r);
+        c->pp_half_r2 = 0.5 * r * r;
+        c->pp_r2 = r * r;
+        c->pp_inv_r2 = 1. / (r * r);
+        c->pp_r_AZ13 = r * c->pp_AZ13;
+        c->pp_15_Z13 = 1.5 * Z13;
+        c->pp_cZ = 1.794664E-34 * (double)Z;
+        c->pp_gamma1 = (Z == 1) ? 4.4E-05 : 1.95E-05;
+        c->pp_gamma2 = (Z == 1) ? 4.8E-05 : 5.30E-05;
+    }
+    { // dcs.hh:290, 313-315, 370-374
+        const double M = 0.931494, mpi = 0.134977;
+        c->ph_logA = log(A);
+        c->ph_a_low = exp(-0.1 * log(A));
+        c->ph_q_min = mpi * (1.0 + 0.5 * mpi / M);
+        c->ph_log_q02 = log(0.52544 / 0.06527);
+        c->ph_inv_log_q02 = 1. / c->ph_log_q02;
+    }
+    { // dcs.hh:422, 435-436
+        c->io_Wmin = 0.62 * I;
+        const double m1 = mass - me;
+        c->io_k_rad = 0.5 * m1 * m1 / me;
+        c->io_cZA = 1.535336E-05 * (double)Z / A;
+    }
+}
 
 #ifdef __cplusplus
 }

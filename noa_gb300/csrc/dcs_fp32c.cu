@@ -1,0 +1,242 @@
+/*
+ * FP32-compensated DCS kernels (precision NOA_DCS_FP32C) for sm_103a.
+ *
+ * One kernel shape for all four processes, built on the compacting kernel of
+ * the FP64 path (dcs_fp64.cu) with a second queue:
+ *
+ *   1. a CTA classifies a 1024-pair tile with the exact kinematic bounds
+ *      (pair production, photonuclear; bremsstrahlung and ionisation are
+ *      evaluated for every pair), writes the zeros, and appends the open
+ *      pairs to the shared-memory work queue;
+ *   2. whenever the work queue holds 256 pairs, each thread pops one and
+ *      evaluates it in FP32 (dcs_fp32c.cuh), which also returns an estimate
+ *      of its relative error; results within `tol` are written, the others
+ *      are appended (warp-aggregated) to a shared-memory redo queue;
+ *   3. whenever the redo queue holds 256 pairs, each thread pops one and
+ *      evaluates it in FP64 (dcs_fp64.cuh).
+ *
+ * FP64 work is thus proportional to the redo fraction (0-4% of open pairs
+ * at tol = 1e-6), and every warp of every phase runs with all lanes busy.
+ * No global scratch.
+ */
+#include "dcs_fp32c.cuh"
+#include "dcs_fp64.cuh"
+#include "dcs_launch.h"
+
+#include <cuda_runtime.h>
+
+namespace noa_dcs {
+
+constexpr int F_THREADS = 256;
+constexpr int F_ITEMS = 4;
+constexpr int F_TILE = F_THREADS * F_ITEMS;
+constexpr int F_QCAP = F_TILE + F_THREADS;
+constexpr int F_RCAP = 2 * F_THREADS;
+
+template <int PROC>
+__device__ __forceinline__ double eval32(double K, double q, const noa_dcs_consts &c, float &est) {
+    if (PROC == NOA_DCS_PROC_BREMS)
+        return brems_fp32c(K, q, c, est);
+    else if (PROC == NOA_DCS_PROC_PPROD)
+        return pprod_fp32c<false>(K, q, c, est);
+    else if (PROC == NOA_DCS_PROC_PHOTO)
+        return photo_fp32c<false>(K, q, c, est);
+    else
+        return ion_fp32c(K, q, c, est);
+}
+
+template <int PROC>
+__device__ __forceinline__ double eval64(double K, double q, const noa_dcs_consts &c) {
+    if (PROC == NOA_DCS_PROC_BREMS)
+        return brems_fp64(K, q, c);
+    else if (PROC == NOA_DCS_PROC_PPROD)
+        return pprod_fp64(K, q, c);
+    else if (PROC == NOA_DCS_PROC_PHOTO)
+        return photo_fp64(K, q, c);
+    else
+        return ion_fp64(K, q, c);
+}
+
+template <int PROC>
+__device__ __forceinline__ bool open32(double K, double q, const noa_dcs_consts &c) {
+    if (PROC == NOA_DCS_PROC_PPROD)
+        return pprod_live(K, q, c);
+    else if (PROC == NOA_DCS_PROC_PHOTO)
+        return photo_live(K, q, c);
+    else
+        return true;
+}
+
+__device__ __forceinline__ int scan_block(int v, int *warp_tot, int *total) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    int x = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const int y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o)
+            x += y;
+    }
+    if (lane == 31)
+        warp_tot[warp] = x;
+    __syncthreads();
+    if (warp == 0) {
+        const int w = lane < (F_THREADS >> 5) ? warp_tot[lane] : 0;
+        int s = w;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int y = __shfl_up_sync(0xffffffffu, s, o);
+            if (lane >= o)
+                s += y;
+        }
+        if (lane < (F_THREADS >> 5))
+            warp_tot[lane] = s - w;
+        if (lane == 31)
+            *total = s;
+    }
+    __syncthreads();
+    return warp_tot[warp] + x - v;
+}
+
+struct Queues {
+    double wK[F_QCAP], wQ[F_QCAP];
+    int64_t wI[F_QCAP];
+    double rK[F_RCAP], rQ[F_RCAP];
+    int64_t rI[F_RCAP];
+    int warp_tot[F_THREADS / 32];
+    int tile_open;
+    int rn;
+};
+
+// Evaluates work-queue entry e (if valid) in FP32 and appends it to the redo
+// queue when its error estimate exceeds tol.
+template <int PROC>
+__device__ __forceinline__ void fp32_step(Queues &s, int e, bool valid, double *out, const noa_dcs_consts &c,
+                                          float tol) {
+    bool redo = false;
+    double k = 0., q = 0.;
+    int64_t i = 0;
+    if (valid) {
+        k = s.wK[e];
+        q = s.wQ[e];
+        i = s.wI[e];
+        float est;
+        const double v = eval32<PROC>(k, q, c, est);
+        redo = !(est <= tol);
+        if (!redo)
+            out[i] = v;
+    }
+    const unsigned m = __ballot_sync(0xffffffffu, redo);
+    if (m) {
+        const int lane = threadIdx.x & 31;
+        int base = 0;
+        if (lane == 0)
+            base = atomicAdd(&s.rn, __popc(m));
+        base = __shfl_sync(0xffffffffu, base, 0);
+        if (redo) {
+            const int pos = base + __popc(m & ((1u << lane) - 1u));
+            s.rK[pos] = k;
+            s.rQ[pos] = q;
+            s.rI[pos] = i;
+        }
+    }
+}
+
+template <int PROC>
+__device__ __forceinline__ void drain_redo(Queues &s, double *out, const noa_dcs_consts &c, bool all) {
+    __syncthreads();
+    while (s.rn >= (all ? 1 : F_THREADS)) {
+        const int take = s.rn < F_THREADS ? s.rn : F_THREADS;
+        if ((int)threadIdx.x < take) {
+            const int e = s.rn - take + threadIdx.x;
+            out[s.rI[e]] = eval64<PROC>(s.rK[e], s.rQ[e], c);
+        }
+        __syncthreads();
+        if (threadIdx.x == 0)
+            s.rn -= take;
+        __syncthreads();
+    }
+}
+
+template <int PROC>
+__global__ void __launch_bounds__(F_THREADS) dcs_fp32c_kernel(const double *__restrict__ K,
+                                                              const double *__restrict__ q, double *out, int64_t n,
+                                                              const noa_dcs_consts c, float tol) {
+    __shared__ Queues s;
+    if (threadIdx.x == 0)
+        s.rn = 0;
+    int qn = 0;
+    for (int64_t base = (int64_t)blockIdx.x * F_TILE; base < n; base += (int64_t)gridDim.x * F_TILE) {
+        double k[F_ITEMS], r[F_ITEMS];
+        unsigned open = 0;
+#pragma unroll
+        for (int j = 0; j < F_ITEMS; j++) {
+            const int64_t i = base + j * F_THREADS + threadIdx.x;
+            if (i < n) {
+                k[j] = K[i];
+                r[j] = q[i];
+                if (open32<PROC>(k[j], r[j], c))
+                    open |= 1u << j;
+                else
+                    out[i] = 0.;
+            }
+        }
+        int pos = qn + scan_block(__popc(open), s.warp_tot, &s.tile_open);
+#pragma unroll
+        for (int j = 0; j < F_ITEMS; j++) {
+            if (open & (1u << j)) {
+                s.wK[pos] = k[j];
+                s.wQ[pos] = r[j];
+                s.wI[pos] = base + j * F_THREADS + threadIdx.x;
+                pos++;
+            }
+        }
+        __syncthreads();
+        qn += s.tile_open;
+        while (qn >= F_THREADS) {
+            fp32_step<PROC>(s, qn - F_THREADS + threadIdx.x, true, out, c, tol);
+            qn -= F_THREADS;
+            drain_redo<PROC>(s, out, c, false);
+        }
+    }
+    fp32_step<PROC>(s, threadIdx.x, (int)threadIdx.x < qn, out, c, tol);
+    drain_redo<PROC>(s, out, c, true);
+}
+
+static int sm_count() {
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    return sms > 0 ? sms : 1;
+}
+
+template <int PROC>
+static cudaError_t launch(const double *K, const double *q, double *out, int64_t n, const noa_dcs_consts &c,
+                          float tol, cudaStream_t s) {
+    const int64_t tiles = (n + F_TILE - 1) / F_TILE;
+    const int64_t cap = (int64_t)sm_count() * 4;
+    const int grid = (int)(tiles < cap ? tiles : cap);
+    dcs_fp32c_kernel<PROC><<<grid, F_THREADS, 0, s>>>(K, q, out, n, c, tol);
+    return cudaGetLastError();
+}
+
+} // namespace noa_dcs
+
+using namespace noa_dcs;
+
+cudaError_t noa_dcs_launch_fp32c(int process, const double *K, const double *q, double *out, int64_t n,
+                                 const noa_dcs_consts *c, float tol, cudaStream_t stream) {
+    if (n <= 0)
+        return cudaSuccess;
+    switch (process) {
+    case NOA_DCS_PROC_BREMS:
+        return launch<NOA_DCS_PROC_BREMS>(K, q, out, n, *c, tol, stream);
+    case NOA_DCS_PROC_PPROD:
+        return launch<NOA_DCS_PROC_PPROD>(K, q, out, n, *c, tol, stream);
+    case NOA_DCS_PROC_PHOTO:
+        return launch<NOA_DCS_PROC_PHOTO>(K, q, out, n, *c, tol, stream);
+    case NOA_DCS_PROC_ION:
+        return launch<NOA_DCS_PROC_ION>(K, q, out, n, *c, tol, stream);
+    default:
+        return cudaErrorInvalidValue;
+    }
+}

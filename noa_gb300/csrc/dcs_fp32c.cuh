@@ -1,0 +1,406 @@
+/*
+ * FP32-compensated ("FP32C") forms of the four muon DCS processes.
+ *
+ * The quadrature bodies run in FP32, with compensated node sums.  FP64 is
+ * kept where float would lose the answer: the kinematic bounds (decided
+ * exactly as the reference decides them, so the zero pattern is the
+ * reference's), the kinematic-edge differences E - q, 1 - nu, 2Mq - Q2 and
+ * the node arguments t tmin / log Q2 (formed in double, then split into a
+ * float pair), the kinematic-limit logs log(argmin), log Q2min, log Q2max,
+ * and the final macroscopic scaling (its constants are far below FLT_MIN).
+ *
+ * Reformulations that remove float cancellations, all exact algebra:
+ *  - pair production Be / Bmu, dcs.hh:188-216: the terms
+ *    xi log(1 + 1/xi) - 1 and log(1 + xi)/xi - 1 cancel to O(1/xi) (O(xi)); they
+ *    are evaluated as u H(u) with H(u) = (log1p(u) - u)/u^2 from a fitted
+ *    polynomial (gen_fp32c_poly.py) for u <= 1;
+ *  - pair production Le, dcs.hh:201-202: one log of (AZ13 q/D1)^2 xe/D2;
+ *  - rho = 1 - exp(t tmin) as -expm1, and (1 - rho) as exp(t tmin);
+ *  - photonuclear ALLM, dcs.hh:289-292: W2 - M2 = Q2 (1/x - 1) = 2Mq - Q2, so
+ *    xP = (Q2 + mP2)/(mP2 + 2Mq); t = log(1 + log1p(Q2/Q02)/log(Q02/L2));
+ *    1 - x = (2Mq - Q2)/(2Mq) with 2Mq - Q2 = (2Mq - Q2max) - Q2max expm1(.);
+ *  - cP, aP: 1/(1 + e) - 1 = -e/(1 + e).
+ *
+ * Each evaluation also returns `est`, a running estimate of its relative
+ * float rounding error (a few units of 2^-24 per operation, scaled by the size
+ * of what cancels), or infinity where a branch or clamp of the reference sits
+ * within rounding distance.  When est exceeds the caller's tolerance the
+ * kernel evaluates that pair in FP64 instead.
+ *
+ * Written for host and device (NOA_HD) so that the same source can be
+ * checked against the CPU oracle.
+ */
+#pragma once
+
+#include "dcs_common.cuh"
+
+namespace noa_dcs {
+
+constexpr float U32 = 5.9604645e-08f; // 2^-24
+
+NOA_HD float f_rcp(float x) {
+#if defined(__CUDA_ARCH__)
+    float y = lean64::rcp_approx(x);
+    return fmaf(y, fmaf(-x, y, 1.f), y);
+#else
+    return 1.f / x;
+#endif
+}
+NOA_HD float f_div(float a, float b) { return a * f_rcp(b); }
+NOA_HD float f_clamp0(float v) { return v < 0.f ? 0.f : v; }
+
+// H(u) = (log1p(u) - u) / u^2 on [0, 1] (gen_fp32c_poly.py, 9.7e-9 truncation).
+NOA_HD float poly_H(float u) {
+    float h = 2.873883747e-03f;
+    h = fmaf(h, u, -1.751224284e-02f);
+    h = fmaf(h, u, 4.993118107e-02f);
+    h = fmaf(h, u, -9.202963259e-02f);
+    h = fmaf(h, u, 1.307132827e-01f);
+    h = fmaf(h, u, -1.637850887e-01f);
+    h = fmaf(h, u, 1.995935617e-01f);
+    h = fmaf(h, u, -2.499702413e-01f);
+    h = fmaf(h, u, 3.333324756e-01f);
+    return fmaf(h, u, -4.999999959e-01f);
+}
+
+// Compensated float accumulator (Neumaier's variant of Kahan summation).
+struct KSum {
+    float s = 0.f, c = 0.f;
+    NOA_HD void add(float v) {
+        const float t = s + v;
+        c += (fabsf(s) >= fabsf(v)) ? ((s - t) + v) : ((v - t) + s);
+        s = t;
+    }
+    NOA_HD double value() const { return (double)s + (double)c; }
+};
+
+// exp(uh + ul) and -expm1(uh + ul) for a double argument split into floats.
+NOA_HD void f_exp_split(double u, float &e, float &em1) {
+    const float uh = (float)u;
+    const float ul = (float)(u - (double)uh);
+    const float eh = expf(uh);
+    e = fmaf(eh, ul, eh);
+    em1 = fmaf(eh, ul, expm1f(uh));
+}
+
+// ---------------------------------------------------------------- bremsstrahlung
+NOA_HD double brems_fp32c(double K, double q, const noa_dcs_consts &c, float &est) {
+    est = 0.f;
+    const double E = K + c.mass;
+    const float Ef = (float)E, qf = (float)q;
+    // q < qe_max (physics.hh:142): float decision, exact when close
+    const float qe = f_div(Ef, 1.f + (float)c.br_half_m2 * f_rcp((float)ME * Ef));
+    bool below = qf < qe;
+    if (fabsf(qf - qe) <= 1e-5f * qe)
+        below = brems_below_qe(E, q, c);
+    const float Emq = (float)(E - q);
+    const float sqrte = 1.648721271f;
+    // delta = 0.5 m^2 nu / (E (1 - nu)) = 0.5 m^2 q / (E (E - q))
+    const float delta = (float)c.br_half_m2 * qf * f_rcp(Ef * Emq);
+    const float BZn = (float)c.br_BZ_n, Dn = (float)c.br_D_n, BZe = (float)c.br_BZ_e;
+    const float Phi_n = logf((BZn * ((float)c.mass + delta * (float)c.br_Dn_sqrte_m2)) *
+                             f_rcp(Dn * ((float)ME + delta * sqrte * BZn)));
+    float Phi_e = 0.f;
+    if (below)
+        Phi_e = logf((float)c.br_BZe_mass *
+                     f_rcp((1.f + delta * (float)c.br_phie_factor) * ((float)ME + delta * sqrte * BZe)));
+    const float Zf = (float)c.Zd;
+    const float S = Zf * f_clamp0(Phi_n) + f_clamp0(Phi_e);
+    // 4/3 (1/nu - 1) + nu = 4/3 (E - q)/q + q/E
+    const float fac = 1.33333333f * Emq * f_rcp(qf) + qf * f_rcp(Ef);
+    const float err = Zf * 3.f * U32 + 3.f * U32 + 3.f * U32 * S;
+    est = 2.0f * err * f_rcp(S);  // calibrated against the oracle: max error <= est
+    if (!(S > 0.f) || !(Phi_n > 16.f * U32 || Phi_n < -16.f * U32) ||
+        (below && !(Phi_e > 16.f * U32 || Phi_e < -16.f * U32)))
+        est = INFINITY;
+    return (double)(S * fac) * (c.br_dcs_factor * c.scale_A);
+}
+
+// ---------------------------------------------------------------- pair production
+// CHECKED = false: the caller has already established with the exact bounds
+// that the pair is open, and argmin is then formed in lean arithmetic (its
+// relative error only matters for |tmin| < 1e-6, which is sent to FP64).
+template <bool CHECKED = true>
+NOA_HD double pprod_fp32c(double K, double q, const noa_dcs_consts &c, float &est) {
+    est = 0.f;
+    double argmin;
+    if (CHECKED) {
+        if (q <= 4. * ME)
+            return 0.;
+        if (q >= K + c.pp_kmax_shift)
+            return 0.;
+        argmin = pprod_argmin_exact(K, q, c);
+        if ((argmin >= 1.) || (argmin <= 0.))
+            return 0.;
+    } else {
+        const double gamma = 1. + K * c.inv_mass;
+        const double x0 = 4. * ME * d_rcp(q);
+        const double x1 = 6. * d_rcp(gamma * (gamma - q * c.inv_mass));
+        argmin = (x0 + 2. * (1. - x0) * x1) * d_rcp(1. + (1. - x1) * d_sqrt(1. - x0));
+    }
+    const double mass = c.mass;
+    const double E = K + mass;
+    const double Emq = E - q;
+    // beta = 0.5 nu^2 / (1 - nu) = 0.5 q^2 / (E (E - q))
+    const double beta_d = 0.5 * q * q * d_rcp(E * Emq);
+    const double tmin_d = d_log(argmin);
+    const float tmin = (float)tmin_d;
+    const float beta = (float)beta_d;
+    const float xi_factor = (float)(c.pp_half_r2 * beta_d);
+    const float qf = (float)q;
+    const float AZ13 = (float)c.pp_AZ13, cL = (float)c.pp_cL, cLe = (float)c.pp_cLe;
+    const float rAZ13 = (float)c.pp_r_AZ13, Z13_15 = (float)c.pp_15_Z13, inv_r2 = (float)c.pp_inv_r2;
+    const float b2 = 2.f * beta, b15 = 1.5f * beta, b3 = 3.f * beta, b4 = 4.f * beta;
+    const float GL8W[8] = {0.05061427f, 0.11119052f, 0.15685332f, 0.18134189f,
+                           0.18134189f, 0.15685332f, 0.11119052f, 0.05061427f};
+    const double GL8Xd[8] = {0.01985507, 0.10166676, 0.2372338, 0.40828268,
+                             0.59171732, 0.7627662, 0.89833324, 0.98014493};
+
+    KSum I;
+    float err = 0.f;
+    bool edge = !(fabsf(tmin) > 1e-6f);
+#pragma unroll
+    for (int j = 0; j < 8; j++) {
+        float eps, rho;
+        f_exp_split(GL8Xd[j] * tmin_d, eps, rho);
+        rho = -rho;
+        const float rho2 = rho * rho;
+        const float rho21 = eps * (2.f - eps);
+        const float xi = xi_factor * rho21;
+        const float xi_i = f_rcp(xi);
+        const float opxi = 1.f + xi;
+        const float inv_opxi = f_rcp(opxi);
+        // branch thresholds of the reference (1e3, 1e-3) must be taken as it takes them
+        edge |= fabsf(xi - 1e3f) <= 2e-4f || fabsf(xi - 1e-3f) <= 2e-10f;
+
+        float Be, eBe;
+        if (xi >= 1E+03f) {
+            Be = 0.5f * xi_i * ((3.f - rho2) + b2 * (1.f + rho2));
+            eBe = 2.f * U32 * Be;
+        } else {
+            const float A = (2.f + rho2) * (1.f + beta);
+            float L, G;
+            if (xi >= 1.f) {
+                G = xi_i * poly_H(xi_i);  // xi log(1 + 1/xi) - 1
+                L = xi_i * (1.f + G);     // log(1 + 1/xi)
+            } else {
+                L = log1pf(xi_i);
+                G = xi * L - 1.f;
+            }
+            const float t1 = A * L, t2 = (3.f + rho2) * G, t3 = (rho21 - beta) * inv_opxi;
+            Be = t1 + t2 + t3;
+            eBe = 2.f * U32 * (fabsf(t1) + fabsf(t2) + fabsf(t3) + fabsf(beta) * inv_opxi);
+        }
+        const float Ye = f_div(5.f - rho2 + b4 * (1.f + rho2), 2.f * (1.f + b3) * logf(3.f + xi_i) - rho2 -
+                                                                  b2 * (2.f - rho2));
+        const float xe = opxi * (1.f + Ye);
+        const float cLi = cL * f_rcp(rho21);
+        const float r1 = AZ13 * qf * f_rcp(qf + cLi * xe);
+        const float r2 = xe * f_rcp(1.f + cLe * xe);
+        const float Le = 0.5f * logf(r1 * r1 * r2);
+        const float Phi_e = f_clamp0(Be * Le);
+
+        float Bmu, eBmu;
+        if (xi <= 1E-03f) {
+            Bmu = 0.5f * xi * (5.f - rho2 + beta * (3.f + rho2));
+            eBmu = 2.f * U32 * Bmu;
+        } else {
+            float L1, G2;
+            if (xi <= 1.f) {
+                G2 = xi * poly_H(xi);  // log(1 + xi)/xi - 1
+                L1 = xi * (1.f + G2);  // log(1 + xi)
+            } else {
+                L1 = log1pf(xi);
+                G2 = L1 * xi_i - 1.f;
+            }
+            const float s1 = (1.f + rho2) * (1.f + b15) * L1, s2 = (1.f + b2) * rho21 * G2,
+                        s3 = xi * (rho21 - beta) * inv_opxi;
+            Bmu = s1 - s2 + s3;
+            eBmu = 2.f * U32 * (fabsf(s1) + fabsf(s2) + fabsf(s3) + xi * fabsf(beta) * inv_opxi);
+        }
+        const float Ymu = f_div(4.f + rho2 + b3 * (1.f + rho2),
+                                (1.f + rho2) * (1.5f + b2) * logf(3.f + xi) + 1.f - 1.5f * rho2);
+        const float xmu = opxi * (1.f + Ymu);
+        const float Lmu = logf(rAZ13 * qf * f_rcp(Z13_15 * (qf + cLi * xmu)));
+        const float Phi_mu = f_clamp0(Bmu * Lmu);
+        const float g = -(Phi_e + Phi_mu * inv_r2) * eps * tmin;
+        I.add(g * GL8W[j]);
+        // error of this node: the logs (Le, Lmu) to ~2 u absolute, the B terms as tracked, the rest ~3 u relative
+        const float eg = fabsf(eps * tmin) *
+                         ((Phi_e > 0.f ? fabsf(Be) * 2.f * U32 + fabsf(Le) * eBe : 0.f) +
+                          (Phi_mu > 0.f ? (fabsf(Bmu) * 2.f * U32 + fabsf(Lmu) * eBmu) * inv_r2 : 0.f)) +
+                         fabsf(g) * 3.f * U32;
+        err += eg * GL8W[j];
+        // a screening log near zero decides the clamp; let FP64 decide it
+        edge |= (fabsf(Le) < 64.f * U32) || (fabsf(Lmu) < 64.f * U32);
+    }
+
+    const double gamma = 1. + K * c.inv_mass;
+    float zeta = 0.f;
+    if (!(gamma <= 35.)) {
+        const float gf = (float)gamma, Z13 = (float)c.pp_Z13;
+        zeta = 0.073f * logf(gf * f_rcp(1.f + (float)c.pp_gamma1 * gf * Z13 * Z13)) - 0.26f;
+        if (zeta <= 0.f)
+            zeta = 0.f;
+        else
+            zeta = f_div(zeta, 0.058f * logf(gf * f_rcp(1.f + (float)c.pp_gamma2 * gf * Z13)) - 0.14f);
+        edge |= fabsf(gamma - 35.) < 1e-4;
+    }
+    const double Id = I.value();
+    est = edge ? INFINITY : 1.3f * err * f_rcp((float)fabs(Id));  // calibrated: max error <= est
+    const double dcs = c.pp_cZ * (c.Zd + (double)zeta) * Emq * Id * d_rcp(q * E);
+    return (dcs < 0.) ? 0. : dcs * (mass + K) * c.scale_A;
+}
+
+// ---------------------------------------------------------------- photonuclear
+// CHECKED = false: the caller has established that the pair is inside the
+// kinematic window; Q2min / Q2max are then formed in lean arithmetic.
+template <bool CHECKED = true>
+NOA_HD double photo_fp32c(double K, double q, const noa_dcs_consts &c, float &est) {
+    est = 0.f;
+    const double mass = c.mass;
+    const double E = K + mass;
+    double Q2min, Q2max;
+    if (CHECKED) {
+        if (!photo_window(K, q, c, Q2min, Q2max))
+            return 0.;
+    } else {
+        const double yl = q * d_rcp(E);
+        Q2min = mass * mass * yl * yl * d_rcp((E - q) * d_rcp(E));
+        Q2max = 2.0 * PH_M * (q - PH_MPI) - PH_MPI * PH_MPI;
+    }
+    const double pQ2min = d_log(Q2min);
+    const double pQ2max = d_log(Q2max);
+    const double dpQ2 = pQ2max - pQ2min;
+    const double pQ2c = 0.5 * (pQ2max + pQ2min);
+    const double inv_E = d_rcp(E);
+    const float omy = (float)((E - q) * inv_E);  // 1 - y, kinematic edge q -> E
+    const float y = (float)(q * inv_E);
+    const double two_Mq_d = 2. * PH_M * q;
+    const float D = (float)(two_Mq_d - Q2max);  // 2Mq - Q2max = 2 M mpi + mpi^2 up to rounding
+    const float inv_2Mq = (float)d_rcp(two_Mq_d);
+    const float inv_Mq = 2.f * inv_2Mq;
+    const float Q2maxf = (float)Q2max;
+    const float half_dp = (float)(0.5 * dpQ2);
+
+    const float m02 = 0.31985f, mP2 = 49.457f, mR2 = 0.15052f;
+    const float cP1 = 0.28067f, cP2 = 0.22291f, cP3 = 2.1979f;
+    const float aP1 = -0.0808f, aP2 = -0.44812f, aP3 = 1.1709f;
+    const float bP1 = 0.36292f, bP2 = 1.8917f, bP3 = 1.8439f;
+    const float cR1 = 0.80107f, cR2 = 0.97307f, cR3 = 3.4942f;
+    const float aR1 = 0.58400f, aR2 = 0.37888f, aR3 = 2.6063f;
+    const float bR1 = 0.01147f, bR2 = 3.7582f, bR3 = 0.49338f;
+    const float inv_P = (float)d_rcp(49.457 + two_Mq_d);
+    const float inv_R = (float)d_rcp(0.15052 + two_Mq_d);
+    const float inv_Q02 = 1.f / 0.52544f;
+    const float inv_LQ = (float)c.ph_inv_log_q02;
+    const float Af = (float)c.A, logA = (float)c.ph_logA, a_low = (float)c.ph_a_low;
+    const float two_m2 = (float)(2. * mass * mass);
+    const float invEE = (float)(inv_E * inv_E);
+    const float yy = y * y;
+    const float GL9X[9] = {0.0000000000000000f, -0.8360311073266358f, 0.8360311073266358f,
+                           -0.9681602395076261f, 0.9681602395076261f, -0.3242534234038089f,
+                           0.3242534234038089f, -0.6133714327005904f, 0.6133714327005904f};
+    const double GL9Xd[9] = {0.0000000000000000, -0.8360311073266358, 0.8360311073266358,
+                             -0.9681602395076261, 0.9681602395076261, -0.3242534234038089,
+                             0.3242534234038089, -0.6133714327005904, 0.6133714327005904};
+    const float GL9W[9] = {0.3302393550012598f, 0.1806481606948574f, 0.1806481606948574f,
+                           0.0812743883615744f, 0.0812743883615744f, 0.3123470770400029f,
+                           0.3123470770400029f, 0.2606106964029354f, 0.2606106964029354f};
+
+    KSum S;
+    float err = 0.f;
+    bool edge = false;
+#pragma unroll
+    for (int j = 0; j < 9; j++) {
+        float Q2, unused;
+        f_exp_split(pQ2c + 0.5 * dpQ2 * GL9Xd[j], Q2, unused);
+        const float invQ2 = f_rcp(Q2);
+        const float x = 0.5f * Q2 * inv_Mq;
+        // ALLM, dcs.hh:288-306
+        const float t = log1pf(log1pf(Q2 * inv_Q02) * inv_LQ);
+        const float xP = (Q2 + mP2) * inv_P;
+        const float xR = (Q2 + mR2) * inv_R;
+        const float lnt = logf(t);
+        const float ecP = expf(cP3 * lnt), eaP = expf(aP3 * lnt);
+        const float cP = cP1 - (cP1 - cP2) * ecP * f_rcp(1.f + ecP);
+        const float aP = aP1 - (aP1 - aP2) * eaP * f_rcp(1.f + eaP);
+        const float bP = bP1 + bP2 * expf(bP3 * lnt);
+        const float cR = cR1 + cR2 * expf(cR3 * lnt);
+        const float aR = aR1 + aR2 * expf(aR3 * lnt);
+        const float bR = bR1 + bR2 * expf(bR3 * lnt);
+        // 1 - x = (2Mq - Q2)/(2Mq), 2Mq - Q2 = D + Q2max (1 - exp(-dpQ2 (1 - t_j)/2))
+        const float om = (D - Q2maxf * expm1f(-half_dp * (1.f - GL9X[j]))) * inv_2Mq;
+        const float l1x = logf(om);
+        const float lxP = logf(xP), lxR = logf(xR);
+        const float eP = aP * lxP + bP * l1x, eR = aR * lxR + bR * l1x;
+        const float F2P = cP * expf(eP);
+        const float F2R = cR * expf(eR);
+        const float F2p = Q2 * f_rcp(Q2 + m02) * (F2P + F2R);
+        // float error of F2: the exponents carry ~3 u of each |term|
+        const float eF2 = U32 *
+                              (F2P * (fabsf(aP * lxP) + fabsf(bP * l1x) + 2.f) +
+                               F2R * (fabsf(aR * lxR) + fabsf(bR * l1x) + 2.f)) *
+                              f_rcp(F2P + F2R) +
+                          3.f * U32;
+        // DRSS shadowing, dcs.hh:310-319
+        float a = 1.f, ea = 0.f;
+        if (x < 0.0014f)
+            a = a_low;
+        else if (x < 0.04f) {
+            const float ex = (0.069f * (logf(x) * 0.4342944819f) + 0.097f) * logA;
+            a = expf(ex);
+            ea = U32 * (fabsf(ex) + 1.f);
+        }
+        edge |= fabsf(x - 0.0014f) <= 1e-6f * 0.0014f || fabsf(x - 0.04f) <= 1e-6f * 0.04f;
+        const float F2A = 0.5f * Af * a * (2.f + x * (-1.85f + x * (2.45f + x * (-2.35f + x)))) * F2p;
+        // Whitlow R, dcs.hh:322-332
+        const bool low = Q2 < 0.3f;
+        const float q2 = low ? 0.3f : Q2;
+        const float inv_q2 = low ? 3.33333333f : invQ2;
+        const float theta = 1.f + 12.f * q2 * 0.015625f * f_rcp((1.f + q2) * (0.015625f + x * x));
+        const float R = 0.635f * theta * f_rcp(logf(q2 * 25.f)) + 0.5747f * inv_q2 - 0.3534f * f_rcp(0.09f + q2 * q2);
+        // d2sigma, dcs.hh:348-354, without cf / q (applied in double below)
+        const float T2 = 0.5f * (1.f - two_m2 * invQ2) * (yy + Q2 * invEE) * f_rcp(1.f + R);
+        const float X = omy + T2;
+        const float d_a = X * invQ2 * invQ2, d_b = 0.25f * invEE * invQ2;
+        const float dds = d_a - d_b;
+        const float g = F2A * dds * Q2;
+        S.add(g * GL9W[j]);
+        const float e_dds = 2.f * U32 * (fabsf(d_a) + fabsf(d_b)) +
+                            fabsf(d_a) * 3.f * U32 * (fabsf(omy) + fabsf(T2)) * f_rcp(fabsf(X));
+        err += GL9W[j] * (fabsf(g) * (eF2 + ea + 4.f * U32) + fabsf(F2A * Q2) * e_dds);
+    }
+    const double ds_f = S.value();
+    est = edge ? INFINITY : 0.6f * err * f_rcp((float)fabs(ds_f));  // calibrated: max error <= est
+    const double ds = ds_f * 2.603096E-35 * d_rcp(q);
+    return (ds < 0.) ? 0. : 0.5 * ds * dpQ2 * (mass + K) * c.scale_A;
+}
+
+// ---------------------------------------------------------------- ionisation
+// The close-collision cross-section keeps FP64: its a1 + a2/q cancels by up to
+// gamma^2 near q = W_max (dcs.hh:427-431).  Only the radiative correction, a
+// relative term of O(1e-2), runs in FP32.
+NOA_HD double ion_fp32c(double K, double q, const noa_dcs_consts &c, float &est) {
+    est = 0.f;
+    const double mass = c.mass;
+    const double P2 = K * (K + 2. * mass);
+    const double E = K + mass;
+    const double Wmax = ion_wmax(P2, E, c);
+    if ((Wmax < NOA_X_FRACTION * K) || (q > Wmax))
+        return 0.;
+    if (q <= c.io_Wmin)
+        return 0.;
+    const double inv_P2 = d_rcp(P2);
+    const double inv_q = d_rcp(q);
+    const double cs = c.io_cZA * E * (0.5 * inv_P2 + inv_q * (E * E * inv_P2 * inv_q - d_rcp(Wmax)));
+    float Delta = 0.f;
+    if (K >= c.io_k_rad) {
+        const float L1 = log1pf((float)(q * (2. / ME)));
+        const float Ef = (float)E;
+        Delta = 1.16141E-03f * L1 * (logf(4.f * Ef * (float)(E - q) * (float)c.inv_m2) - L1);
+    }
+    return cs * (1. + (double)Delta);
+}
+
+} // namespace noa_dcs

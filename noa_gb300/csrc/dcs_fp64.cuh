@@ -29,8 +29,7 @@
  */
 #pragma once
 
-#include "dcs_consts.h"
-#include "lean64.cuh"
+#include "dcs_common.cuh"
 
 namespace noa_dcs {
 
@@ -54,9 +53,6 @@ __constant__ double kGL9W[9] = {0.3302393550012598, 0.1806481606948574, 0.180648
                                 0.0812743883615744, 0.0812743883615744, 0.3123470770400029,
                                 0.3123470770400029, 0.2606106964029354, 0.2606106964029354};
 
-constexpr double ME = NOA_ELECTRON_MASS;
-constexpr double NA = NOA_AVOGADRO_NUMBER;
-
 // Clamp of the reference's `if (v < 0.) v = 0.;` that keeps NaN.
 __device__ __forceinline__ double clamp0(double v) {
     const long long b = __double_as_longlong(v);
@@ -76,7 +72,7 @@ __device__ __forceinline__ double brems_fp64(double K, double q, const noa_dcs_c
     bool below = q < qe_lean;
     const long long dist = __double_as_longlong(q) - __double_as_longlong(qe_lean);
     if (dist < 64 && dist > -64)
-        below = q < __ddiv_rn(E, __dadd_rn(1., __ddiv_rn(c.br_half_m2, __dmul_rn(ME, E))));
+        below = brems_below_qe(E, q, c);
     const double nu = __ddiv_rn(q, E);  // as the reference: 1 - nu cancels as q -> E
     const double delta = delta_factor * nu * lean_rcp(1. - nu);
     const double Phi_n = clamp0(lean_log(c.br_BZ_n * (mass + delta * c.br_Dn_sqrte_m2) *
@@ -90,16 +86,6 @@ __device__ __forceinline__ double brems_fp64(double K, double q, const noa_dcs_c
 }
 
 // ---------------------------------------------------------------- pair production
-// Lower end of the t-integral, argmin of dcs.hh:169-173, in the reference's
-// IEEE arithmetic (its rounding decides both the bound and tmin near 1).
-__device__ __forceinline__ double pprod_argmin_exact(double K, double q, const noa_dcs_consts &c) {
-    const double gamma = __dadd_rn(1., __ddiv_rn(K, c.mass));
-    const double x0 = __ddiv_rn(4. * ME, q);
-    const double x1 = __ddiv_rn(6., __dmul_rn(gamma, __dsub_rn(gamma, __ddiv_rn(q, c.mass))));
-    return __ddiv_rn(__dadd_rn(x0, __dmul_rn(__dmul_rn(2., __dsub_rn(1., x0)), x1)),
-                     __dadd_rn(1., __dmul_rn(__dsub_rn(1., x1), __dsqrt_rn(__dsub_rn(1., x0)))));
-}
-
 __device__ __forceinline__ bool pprod_live(double K, double q, const noa_dcs_consts &c) {
     if (q <= 4. * ME)
         return false;
@@ -191,28 +177,6 @@ __device__ __forceinline__ double pprod_fp64(double K, double q, const noa_dcs_c
 }
 
 // ---------------------------------------------------------------- photonuclear
-constexpr double PH_M = 0.931494;
-constexpr double PH_MPI = 0.134977;
-
-// Photonuclear kinematic window, dcs.hh:357-381, in the reference's IEEE
-// arithmetic.  Returns false when the reference returns 0 before its
-// quadrature; on true, Q2min / Q2max are the reference's values.
-__device__ __forceinline__ bool photo_window(double K, double q, const noa_dcs_consts &c, double &Q2min,
-                                             double &Q2max) {
-    if ((q < 1.) || (q < 2E-03 * K))
-        return false;
-    const double mass = c.mass;
-    const double E = K + mass;
-    if ((q >= (E - mass)) || (q <= c.ph_q_min))
-        return false;
-    const double y = __ddiv_rn(q, E);
-    Q2min = __ddiv_rn(__dmul_rn(__dmul_rn(__dmul_rn(mass, mass), y), y), __dsub_rn(1., y));
-    Q2max = __dsub_rn(__dmul_rn(2.0 * PH_M, q - PH_MPI), PH_MPI * PH_MPI);
-    if ((Q2max < Q2min) | (Q2min < 0))
-        return false;
-    return true;
-}
-
 __device__ __forceinline__ bool photo_live(double K, double q, const noa_dcs_consts &c) {
     double a, b;
     return photo_window(K, q, c, a, b);
@@ -301,7 +265,7 @@ __device__ __forceinline__ double ion_fp64(double K, double q, const noa_dcs_con
     const double mass = c.mass;
     const double P2 = K * (K + 2. * mass);
     const double E = K + mass;
-    const double Wmax = __ddiv_rn(2. * ME * P2, __dadd_rn(__dmul_rn(mass, mass), __dmul_rn(ME, ME + 2. * E)));
+    const double Wmax = ion_wmax(P2, E, c);
     if ((Wmax < NOA_X_FRACTION * K) || (q > Wmax))
         return 0.;
     if (q <= c.io_Wmin)

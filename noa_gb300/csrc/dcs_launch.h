@@ -17,3 +17,11 @@
 /* FP64 kernels (dcs_fp64.cu).  Arguments are already validated. */
 cudaError_t noa_dcs_launch_fp64(int process, const double *K, const double *q, double *out, int64_t n,
                                 const noa_dcs_consts *c, cudaStream_t stream);
+
+/* FP32-compensated kernels (dcs_fp32c.cu): pairs whose estimated relative
+ * error exceeds tol are recomputed in FP64. */
+cudaError_t noa_dcs_launch_fp32c(int process, const double *K, const double *q, double *out, int64_t n,
+                                 const noa_dcs_consts *c, float tol, cudaStream_t stream);
+
+/* Default FP32C tolerance: relative error bound per pair. */
+#define NOA_DCS_FP32C_DEFAULT_TOL 1e-6f
