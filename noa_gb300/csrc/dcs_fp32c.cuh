@@ -400,6 +400,7 @@ NOA_HD double ion_fp32c(double K, double q, const noa_dcs_consts &c, float &est)
         const float Ef = (float)E;
         Delta = 1.16141E-03f * L1 * (logf(4.f * Ef * (float)(E - q) * (float)c.inv_m2) - L1);
     }
+    est = fabsf(Delta) * 8.f * U32;  // the float part is Delta, relative to 1 + Delta
     return cs * (1. + (double)Delta);
 }
 

@@ -91,17 +91,18 @@ __device__ __forceinline__ bool pprod_live(double K, double q, const noa_dcs_con
         return false;
     if (q >= K + c.pp_kmax_shift)
         return false;
-    // cheap estimate of argmin; exact only where the decision is close
-    const double gamma = 1. + K * c.inv_mass;
-    const double x0 = 4. * ME * lean_rcp(q);
-    const double x1 = 6. * lean_rcp(gamma * (gamma - q * c.inv_mass));
-    const double a = (x0 + 2. * (1. - x0) * x1) * lean_rcp(1. + (1. - x1) * lean64::lean_sqrt(1. - x0));
-    const long long d1 = __double_as_longlong(a) - __double_as_longlong(1.0);
-    if ((d1 < 256 && d1 > -256) || !(fabs(a) > 1e-12)) {
+    // argmin in float (K - q formed in double: gamma - q/m = 1 + (K - q)/m);
+    // the reference's IEEE value decides only within 1e-5 of a bound
+    const float im = (float)c.inv_mass;
+    const float x0 = (float)(4. * ME) * lean64::rcp_approx((float)q);
+    const float gamma = 1.f + (float)K * im;
+    const float x1 = 6.f * lean64::rcp_approx(gamma * (1.f + (float)(K - q) * im));
+    const float a = (x0 + 2.f * (1.f - x0) * x1) * lean64::rcp_approx(1.f + (1.f - x1) * sqrtf(fmaxf(1.f - x0, 0.f)));
+    if (!(fabsf(a - 1.f) > 1e-5f) || !(a > 1e-30f && a < 1e30f) || !(x0 < 0.9f)) {
         const double am = pprod_argmin_exact(K, q, c);
         return !((am >= 1.) || (am <= 0.));
     }
-    return !((a >= 1.) || (a <= 0.));
+    return a < 1.f;
 }
 
 __device__ __forceinline__ double pprod_fp64(double K, double q, const noa_dcs_consts &c) {
