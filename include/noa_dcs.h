@@ -103,6 +103,41 @@ int noa_dcs_cuda_vmap_fp32c(int process, double *result, const double *K, const 
 int noa_dcs_vmap_host(int process, int precision, double *result, const double *K, const double *q, int64_t n,
                       const noa_dcs_element *element, double mass);
 
+/* ---- batched multi-element engine (no counterpart in the reference, which
+ * evaluates one element per call).  One persistent launch evaluates one
+ * process for n_segments (1..16) elements; segment s has counts[s] pairs
+ * stored back to back in K, q and result (device buffers), element
+ * elements[s].  CTAs take tiles from a global counter, so uneven segments
+ * balance on the GPU.  The plan owns that counter (allocated at creation;
+ * execution allocates nothing) and, after the first execute_graph with a
+ * given buffer triple, a CUDA graph of the counter reset and the launch.
+ * A plan is not thread-safe; executions of one plan on different streams
+ * must not overlap. */
+typedef struct noa_dcs_batch_plan noa_dcs_batch_plan;
+
+int noa_dcs_batch_plan_create(noa_dcs_batch_plan **plan, int process, int precision, int n_segments,
+                              const noa_dcs_element *elements, const int64_t *counts, double mass);
+/* Tile shape: threads per CTA (128 or 256), pairs per thread per tile (1..8),
+ * resident CTAs per SM (clamped to the occupancy limit). */
+int noa_dcs_batch_plan_set_tile(noa_dcs_batch_plan *plan, int threads, int items, int ctas_per_sm);
+int noa_dcs_batch_plan_get_tile(const noa_dcs_batch_plan *plan, int *threads, int *items, int *ctas_per_sm);
+/* FP32C plans: per-pair relative error tolerance (default 1e-6). */
+int noa_dcs_batch_plan_set_tolerance(noa_dcs_batch_plan *plan, float tolerance);
+/* Times every tile shape of the search space on the first sample_per_segment
+ * pairs of each segment (all pairs if <= 0), on these buffers, and keeps the
+ * fastest.  Writes (part of) result. */
+int noa_dcs_batch_plan_autotune(noa_dcs_batch_plan *plan, double *result, const double *K, const double *q,
+                                void *stream, int64_t sample_per_segment);
+/* Enqueues the counter reset and the launch on stream. */
+int noa_dcs_batch_plan_execute(noa_dcs_batch_plan *plan, double *result, const double *K, const double *q,
+                               void *stream);
+/* Same work as one CUDA graph launch (captured on first use per buffer triple). */
+int noa_dcs_batch_plan_execute_graph(noa_dcs_batch_plan *plan, double *result, const double *K, const double *q,
+                                     void *stream);
+int noa_dcs_batch_plan_destroy(noa_dcs_batch_plan *plan);
+/* Message of the last failed batch-plan call on this host thread. */
+const char *noa_dcs_batch_last_error(void);
+
 /* Frees the host-path staging buffers of the current device (they are
  * otherwise kept for reuse until the process exits). */
 int noa_dcs_release_staging(void);

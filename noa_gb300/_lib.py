@@ -55,6 +55,15 @@ SIGNATURES = {
     "noa_dcs_abi_version": (_INT, []),
     "noa_dcs_probe_fma": (_INT, [_INT, _P, _INT, _INT, ctypes.POINTER(_D), _P]),
     "noa_dcs_lean64_eval": (_INT, [_INT, _P, _P, _P, _I64, _P]),
+    "noa_dcs_batch_plan_create": (_INT, [ctypes.POINTER(_P), _INT, _INT, _INT, _EP, ctypes.POINTER(_I64), _D]),
+    "noa_dcs_batch_plan_set_tile": (_INT, [_P, _INT, _INT, _INT]),
+    "noa_dcs_batch_plan_get_tile": (_INT, [_P, ctypes.POINTER(_INT), ctypes.POINTER(_INT), ctypes.POINTER(_INT)]),
+    "noa_dcs_batch_plan_set_tolerance": (_INT, [_P, ctypes.c_float]),
+    "noa_dcs_batch_plan_autotune": (_INT, [_P, _P, _P, _P, _P, _I64]),
+    "noa_dcs_batch_plan_execute": (_INT, [_P, _P, _P, _P, _P]),
+    "noa_dcs_batch_plan_execute_graph": (_INT, [_P, _P, _P, _P, _P]),
+    "noa_dcs_batch_plan_destroy": (_INT, [_P]),
+    "noa_dcs_batch_last_error": (ctypes.c_char_p, []),
 }
 
 _lib = None

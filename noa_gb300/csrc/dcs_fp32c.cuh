@@ -40,8 +40,9 @@ constexpr float U32 = 5.9604645e-08f; // 2^-24
 
 NOA_HD float f_rcp(float x) {
 #if defined(__CUDA_ARCH__)
-    float y = lean64::rcp_approx(x);
-    return fmaf(y, fmaf(-x, y, 1.f), y);
+    const float y = lean64::rcp_approx(x);
+    // one Newton step; 1/0, 1/inf and NaN keep the approximation's IEEE value
+    return (fabsf(y) < INFINITY && y != 0.f) ? fmaf(y, fmaf(-x, y, 1.f), y) : y;
 #else
     return 1.f / x;
 #endif
@@ -113,7 +114,8 @@ NOA_HD double brems_fp32c(double K, double q, const noa_dcs_consts &c, float &es
     if (!(S > 0.f) || !(Phi_n > 16.f * U32 || Phi_n < -16.f * U32) ||
         (below && !(Phi_e > 16.f * U32 || Phi_e < -16.f * U32)))
         est = INFINITY;
-    return (double)(S * fac) * (c.br_dcs_factor * c.scale_A);
+    const double dcs = (double)(S * fac) * (c.br_dcs_factor * c.scale_A);
+    return (dcs < 0.) ? 0. : dcs;
 }
 
 // ---------------------------------------------------------------- pair production

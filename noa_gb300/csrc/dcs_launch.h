@@ -14,6 +14,8 @@
 #define NOA_DCS_PROC_PHOTO NOA_DCS_PHOTONUCLEAR
 #define NOA_DCS_PROC_ION NOA_DCS_IONISATION
 
+#define NOA_DCS_MAX_SEGMENTS 16
+
 /* FP64 kernels (dcs_fp64.cu).  Arguments are already validated. */
 cudaError_t noa_dcs_launch_fp64(int process, const double *K, const double *q, double *out, int64_t n,
                                 const noa_dcs_consts *c, cudaStream_t stream);
@@ -25,3 +27,13 @@ cudaError_t noa_dcs_launch_fp32c(int process, const double *K, const double *q, 
 
 /* Default FP32C tolerance: relative error bound per pair. */
 #define NOA_DCS_FP32C_DEFAULT_TOL 1e-6f
+
+/* Batched engine (dcs_batched.cuh): launch one instantiation.  params points
+ * to a noa_dcs::BatchParams; threads is 128 or 256. */
+cudaError_t noa_dcs_batched_launch64(int process, int threads, const void *params, int grid, size_t smem,
+                                     cudaStream_t stream);
+cudaError_t noa_dcs_batched_launch32(int process, int threads, const void *params, int grid, size_t smem,
+                                     cudaStream_t stream);
+/* Resident CTAs per SM of one instantiation at the given dynamic smem. */
+int noa_dcs_batched_occupancy64(int process, int threads, size_t smem);
+int noa_dcs_batched_occupancy32(int process, int threads, size_t smem);
