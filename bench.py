@@ -54,6 +54,7 @@ def parse_args():
     ap.add_argument("--n", type=int, default=N_PAIRS)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-batched", action="store_true")
     return ap.parse_args()
 
 
@@ -250,6 +251,45 @@ def time_fp32c(lib, torch, tk, tq, ref_outs, n, el, mass, stream, args, fp64_s):
     return res
 
 
+def time_batched(torch, args):
+    """Batched multi-element form: the 10 elements Z in {1,6,8,11,13,14,20,26,
+    29,82} with seeded uneven counts (log-uniform in [1e4, 3e7]) in one
+    persistent launch per process, tile shape from the autotuner, replayed as
+    a CUDA graph; FP64 and FP32C."""
+    from noa_gb300.batched import BatchPlan, batch_inputs
+    from noa_gb300.elements import BATCH_Z, ELEMENTS, MUON_MASS
+    from noa_gb300.workload import element_counts
+    counts = [int(c) for c in element_counts()]
+    K, q = batch_inputs(BATCH_Z, counts)
+    tk, tq = torch.from_numpy(K).cuda(), torch.from_numpy(q).cuda()
+    out = torch.empty_like(tk)
+    n = tk.numel()
+    res = {"elements_Z": list(BATCH_Z), "counts": counts, "total_pairs": n}
+    stream = torch.cuda.current_stream()
+    for precision in ("fp64", "fp32c"):
+        per = {}
+        for p, name in enumerate(PROCESSES):
+            with BatchPlan(p, [ELEMENTS[z] for z in BATCH_Z], counts, MUON_MASS, precision) as plan:
+                tile = plan.autotune(out, tk, tq, sample_per_segment=1 << 17, cache=None)
+                for _ in range(max(1, args.warmup)):
+                    plan.execute_graph(out, tk, tq)
+                s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                steps = max(1, min(args.steps, 5))
+                torch.cuda.synchronize()
+                s.record(stream)
+                for _ in range(steps):
+                    plan.execute_graph(out, tk, tq)
+                e.record(stream)
+                torch.cuda.synchronize()
+                t = s.elapsed_time(e) * 1e-3 / steps
+                per[name] = {"evals_per_s": n / t, "ms_per_launch": 1e3 * t,
+                             "tile": {"threads": tile[0], "items": tile[1], "ctas_per_sm": tile[2]}}
+        total_ms = sum(v["ms_per_launch"] for v in per.values())
+        per["all_processes"] = {"evals_per_s": 4 * n / (total_ms * 1e-3)}
+        res[precision] = per
+    return res
+
+
 def load_traffic():
     path = os.path.join(ROOT, "profiles", "traffic.json")
     try:
@@ -382,6 +422,8 @@ def run_ours(args):
         "clocks": clocks.summary(),
         "gpu_launches": 4 * args.steps,
     }
+    if not args.no_batched:
+        line["batched"] = time_batched(torch, args)
     if not args.no_cpu_baseline and world == 1:
         cb = cpu_reference_rate(min(n, 1_000_000))
         line["cpu_baseline"] = {"value": cb["value"], "unit": "evals/s", "cores": cb["cores"], "kind": "port",
