@@ -138,6 +138,25 @@ int noa_dcs_batch_plan_destroy(noa_dcs_batch_plan *plan);
 /* Message of the last failed batch-plan call on this host thread. */
 const char *noa_dcs_batch_last_error(void);
 
+/* Allocation-free batched evaluation (no counterpart in the reference): the
+ * work of one batch plan execution -- process, precision (FP32C at tolerance
+ * 1e-6), segments (at most 16: larger counts of segments are rejected with
+ * NOA_DCS_ERROR_INVALID_VALUE) -- without a plan and without allocating
+ * anything.  For callers that may not allocate device memory during the
+ * call: code that runs it inside its own stream capture, where cudaMalloc is
+ * forbidden, or a host application that owns all device memory through its
+ * own arena.  The engine's one piece of scratch, a tile counter, lives in a
+ * 256-byte static device array that every device loading the library keeps
+ * until exit; each call zeroes it on `stream` before the launch.  All calls
+ * share that array: calls whose work overlaps on the GPU (different streams,
+ * or different host threads) race and must be serialised by the caller.  The
+ * first call on each device looks up the array's device address (with that
+ * device current) and must come before any stream capture.  Tile shape is
+ * fixed (256 threads x 4 pairs, 2 CTAs per SM).  Buffers as for the plan. */
+int noa_dcs_cuda_vmap_batched_noalloc(int process, int precision, int n_segments, const noa_dcs_element *elements,
+                                      const int64_t *counts, double mass, double *result, const double *K,
+                                      const double *q, void *stream);
+
 /* Frees the host-path staging buffers of the current device (they are
  * otherwise kept for reuse until the process exits). */
 int noa_dcs_release_staging(void);

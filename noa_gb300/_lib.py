@@ -64,6 +64,7 @@ SIGNATURES = {
     "noa_dcs_batch_plan_execute_graph": (_INT, [_P, _P, _P, _P, _P]),
     "noa_dcs_batch_plan_destroy": (_INT, [_P]),
     "noa_dcs_batch_last_error": (ctypes.c_char_p, []),
+    "noa_dcs_cuda_vmap_batched_noalloc": (_INT, [_INT, _INT, _INT, _EP, ctypes.POINTER(_I64), _D, _P, _P, _P, _P]),
 }
 
 _lib = None

@@ -16,6 +16,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <mutex>
 #include <new>
 
 using noa_dcs::BatchParams;
@@ -352,3 +353,98 @@ int noa_dcs_batch_plan_destroy(noa_dcs_batch_plan *p) {
 const char *noa_dcs_batch_last_error(void) { return g_err; }
 
 } // extern "C"
+
+// ---------------------------------------------------------------- allocation-free batched entry point
+//
+// Some callers may not allocate device memory during a call: a transport
+// code that evaluates cross-sections from inside its own CUDA-graph capture
+// (cudaMalloc is not allowed while a stream is being captured), or a host
+// application that has reserved the GPU's memory for its own arena and owns
+// every allocation.  For them the batched engine also runs with its only
+// scratch -- the 64-bit tile counter -- in the static device array below
+// instead of in a plan.  Every device that loads this library holds these
+// 256 bytes until the process exits.
+
+#define NOA_DCS_NOALLOC_SCRATCH_WORDS 32 /* 256 bytes; the engine uses word 0 */
+
+static __device__ __align__(256) unsigned long long noa_dcs_noalloc_scratch[NOA_DCS_NOALLOC_SCRATCH_WORDS];
+
+namespace {
+
+constexpr int kNoallocDevices = 64;
+std::mutex g_noalloc_mu;
+unsigned long long *g_noalloc_addr[kNoallocDevices] = {};
+
+// Device address of the static scratch on the current device.  The symbol's
+// host-side name is not a device address, so the address is looked up once
+// per device, with that device current, and cached.
+int noalloc_scratch(int device, unsigned long long **out) {
+    std::lock_guard<std::mutex> lock(g_noalloc_mu);
+    if (!g_noalloc_addr[device]) {
+        void *ptr = nullptr;
+        const cudaError_t e = cudaGetSymbolAddress(&ptr, noa_dcs_noalloc_scratch);
+        if (e != cudaSuccess || !ptr)
+            return bfail(NOA_DCS_ERROR_CUDA, "cudaGetSymbolAddress(noa_dcs_noalloc_scratch)", e);
+        g_noalloc_addr[device] = static_cast<unsigned long long *>(ptr);
+    }
+    *out = g_noalloc_addr[device];
+    return NOA_DCS_SUCCESS;
+}
+
+} // namespace
+
+extern "C" int noa_dcs_cuda_vmap_batched_noalloc(int process, int precision, int n_segments,
+                                                 const noa_dcs_element *elements, const int64_t *counts,
+                                                 double mass, double *result, const double *K, const double *q,
+                                                 void *stream) {
+    g_err[0] = '\0';
+    if (process < 0 || process > 3 || (precision != NOA_DCS_FP64 && precision != NOA_DCS_FP32C))
+        return bfail(NOA_DCS_ERROR_INVALID_VALUE, "unknown process or precision");
+    if (n_segments < 1 || !elements || !counts)
+        return bfail(NOA_DCS_ERROR_INVALID_VALUE, "need at least one segment with its element and count");
+    if (n_segments > NOA_DCS_MAX_SEGMENTS)
+        return bfail(NOA_DCS_ERROR_INVALID_VALUE,
+                     "too many segments for the allocation-free entry point (maximum 16 per call)");
+    if (!std::isfinite(mass) || !(mass > 0.))
+        return bfail(NOA_DCS_ERROR_INVALID_VALUE, "invalid particle mass");
+    // The plan object on the stack: no host or device allocation.
+    noa_dcs_batch_plan p;
+    std::memset(&p.params, 0, sizeof p.params);
+    for (int s = 0; s < n_segments; s++) {
+        const noa_dcs_element &el = elements[s];
+        if (!std::isfinite(el.A) || !(el.A > 0.) || !std::isfinite(el.I) || !(el.I > 0.) || el.Z < 1)
+            return bfail(NOA_DCS_ERROR_INVALID_ELEMENT, "invalid element");
+        if (counts[s] < 0)
+            return bfail(NOA_DCS_ERROR_INVALID_VALUE, "negative segment count");
+    }
+    cudaError_t e = cudaGetDevice(&p.device);
+    if (e == cudaSuccess)
+        e = cudaDeviceGetAttribute(&p.sms, cudaDevAttrMultiProcessorCount, p.device);
+    if (e != cudaSuccess)
+        return bfail(NOA_DCS_ERROR_CUDA, "device query", e);
+    if (p.device < 0 || p.device >= kNoallocDevices)
+        return bfail(NOA_DCS_ERROR_INVALID_VALUE, "device ordinal out of range");
+    p.process = process;
+    p.precision = precision;
+    p.params.n_seg = n_segments;
+    p.params.tol = NOA_DCS_FP32C_DEFAULT_TOL;
+    for (int s = 0; s < n_segments; s++) {
+        p.params.seg_begin[s + 1] = p.params.seg_begin[s] + counts[s];
+        noa_dcs_fill_consts(&p.params.consts[s], elements[s].A, elements[s].I, elements[s].Z, mass);
+    }
+    // Fixed tile shape (the plan default): 256 threads x 4 pairs, 2 CTAs per
+    // SM; its 43 KB of shared memory needs no opt-in attribute.
+    p.threads = 256;
+    p.items = 4;
+    p.ctas_per_sm = 2;
+    set_tiles(&p);
+    int st = check_buffers(&p, result, K, q);
+    if (st)
+        return st;
+    if (p.params.seg_begin[n_segments] == 0)
+        return NOA_DCS_SUCCESS;
+    if ((st = noalloc_scratch(p.device, &p.params.counter)))
+        return st;
+    // launch() zeroes the counter on the stream before the kernel.
+    return launch(&p, result, K, q, (cudaStream_t)stream);
+}
