@@ -86,6 +86,18 @@ int noa_dcs_cuda_vmap_ionisation(double *result, const double *K, const double *
 int noa_dcs_cuda_vmap(int process, int precision, double *result, const double *K, const double *q, int64_t n,
                       const noa_dcs_element *element, double mass, void *stream);
 
+/* Recoil-energy integrals per kinetic energy, the GPU form of
+ * dcs::vmap_integral(dcs::recoil_integral(dcs::<process>, integrand))
+ * (dcs.hh:89-130, 955-1001):
+ *   result[i] = int_{K xlow}^{K} q^(1+moment) dsigma/dq(K, q) dq / (K + mass),
+ * K = K[i], moment 0 = DEL (del_integrand), 1 = CEL (cel_integrand), with
+ * the reference's composite 6-node Gauss-Legendre rule over log q on
+ * ceil(min_points/6) intervals (min_points in 1..1536; the reference's tests
+ * use 180, xlow = X_FRACTION = 0.05), and ionisation's closed form below its
+ * radiative-correction threshold.  FP64; K and result are device buffers. */
+int noa_dcs_cuda_recoil_integral(int process, int moment, double *result, const double *K, int64_t n, double xlow,
+                                 const noa_dcs_element *element, double mass, int32_t min_points, void *stream);
+
 /* FP32-compensated form with an explicit tolerance: every pair whose
  * estimated relative error exceeds `tolerance` (0 < tolerance < 1) is
  * recomputed in FP64.  noa_dcs_cuda_vmap with NOA_DCS_FP32C uses 1e-6.

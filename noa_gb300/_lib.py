@@ -49,6 +49,7 @@ SIGNATURES = {
     "noa_dcs_cuda_vmap": (_INT, [_INT, _INT, _P, _P, _P, _I64, _EP, _D, _P]),
     "noa_dcs_cuda_vmap_fp32c": (_INT, [_INT, _P, _P, _P, _I64, _EP, _D, ctypes.c_float, _P]),
     "noa_dcs_vmap_host": (_INT, [_INT, _INT, _P, _P, _P, _I64, _EP, _D]),
+    "noa_dcs_cuda_recoil_integral": (_INT, [_INT, _INT, _P, _P, _I64, _D, _EP, _D, ctypes.c_int32, _P]),
     "noa_dcs_release_staging": (_INT, []),
     "noa_dcs_status_string": (ctypes.c_char_p, [_INT]),
     "noa_dcs_last_error": (ctypes.c_char_p, []),

@@ -190,6 +190,38 @@ int noa_dcs_cuda_vmap_ionisation(double *result, const double *K, const double *
     return noa_dcs_cuda_vmap(NOA_DCS_IONISATION, NOA_DCS_FP64, result, K, q, n, element, mass, stream);
 }
 
+int noa_dcs_cuda_recoil_integral(int process, int moment, double *result, const double *K, int64_t n, double xlow,
+                                 const noa_dcs_element *element, double mass, int32_t min_points, void *stream) {
+    g_last_error[0] = '\0';
+    int st = check_common(process, NOA_DCS_FP64, n, mass);
+    if (st)
+        return st;
+    if ((st = check_element(element)))
+        return st;
+    if (moment != 0 && moment != 1)
+        return fail(NOA_DCS_ERROR_INVALID_VALUE, "moment must be 0 (DEL) or 1 (CEL), got %d", moment);
+    if (min_points < 1 || min_points > 1536)
+        return fail(NOA_DCS_ERROR_INVALID_VALUE, "min_points must lie in 1..1536, got %d", (int)min_points);
+    if (!std::isfinite(xlow) || !(xlow > 0.) || !(xlow <= 1.))
+        return fail(NOA_DCS_ERROR_INVALID_VALUE, "xlow must lie in (0, 1], got %g", xlow);
+    if (n == 0)
+        return NOA_DCS_SUCCESS;
+    int device = 0;
+    cudaError_t e = cudaGetDevice(&device);
+    if (e != cudaSuccess)
+        return cuda_fail(e, "cudaGetDevice");
+    if ((st = check_device_buffer(result, "result", device)) || (st = check_device_buffer(K, "K", device)))
+        return st;
+    if (overlaps_partially(result, K, n))
+        return fail(NOA_DCS_ERROR_OVERLAP, "result partially overlaps K");
+    noa_dcs_consts c;
+    noa_dcs_fill_consts(&c, element->A, element->I, element->Z, mass);
+    e = noa_dcs_launch_recoil_integral(process, moment, K, result, n, xlow, min_points, &c, (cudaStream_t)stream);
+    if (e != cudaSuccess)
+        return cuda_fail(e, "recoil integral launch");
+    return NOA_DCS_SUCCESS;
+}
+
 int noa_dcs_vmap_host(int process, int precision, double *result, const double *K, const double *q, int64_t n,
                       const noa_dcs_element *element, double mass) {
     g_last_error[0] = '\0';

@@ -1,0 +1,270 @@
+/*
+ * Recoil-energy integrals of the DCS per kinetic energy (FP64):
+ *
+ *   DEL: (1/E) int_{K xlow}^{K} q dsigma/dq dq      (moment 0)
+ *   CEL: (1/E) int_{K xlow}^{K} q^2 dsigma/dq dq    (moment 1)
+ *
+ * Reference: recoil_integral (src/noa/pms/dcs.hh:89-105) with del_integrand /
+ * cel_integrand (:107-113), mapped by vmap_integral (:115-130): a composite
+ * 6-node Gauss-Legendre rule (numerics.hh:71-108) over t = log q with
+ * n_itv = ceil(min_points / 6) intervals, i.e. 6 n_itv DCS evaluations per
+ * K; ionisation switches to its closed form below the radiative-correction
+ * threshold (dcs.hh:446-496, 955-1001).
+ *
+ * Kernel: a CTA takes a tile of kpt kinetic energies and all their nodes
+ * (kpt * nodes pairs, at most 1536).  Each pair (K, q_i) is classified with the
+ * process's exact bounds; closed pairs contribute 0, open ones go to the
+ * shared-memory work queue and are evaluated 256 at a time with every lane
+ * busy.  Each weighted node value lands in a shared array indexed by
+ * (K, node), and one thread per K then sums its nodes in node order -- the
+ * reference's own order -- so the result does not depend on scheduling.
+ */
+#include "dcs_fp64.cuh"
+#include "dcs_launch.h"
+
+#include <cuda_runtime.h>
+
+namespace noa_dcs {
+
+constexpr int I_THREADS = 256;
+constexpr int I_PAIRS = 1536;  // pairs per tile (kpt * nodes <= I_PAIRS)
+constexpr int I_QCAP = I_PAIRS + I_THREADS;
+constexpr int I_KMAX = 128;    // kinetic energies per tile at most
+
+__constant__ double kGL6X[6] = {0.03376524, 0.16939531, 0.38069041, 0.61930959, 0.83060469, 0.96623476};
+__constant__ double kGL6W[6] = {0.08566225, 0.18038079, 0.23395697, 0.23395697, 0.18038079, 0.08566225};
+
+struct IntegralParams {
+    const double *K;
+    double *out;
+    int64_t n;
+    double xlow;
+    int nodes;  // 6 * n_itv
+    int n_itv;
+    int kpt;    // kinetic energies per tile
+    int moment; // 0 = DEL, 1 = CEL
+};
+
+template <int PROC>
+__device__ __forceinline__ double i_eval(double K, double q, const noa_dcs_consts &c) {
+    if (PROC == NOA_DCS_PROC_BREMS)
+        return brems_fp64(K, q, c);
+    else if (PROC == NOA_DCS_PROC_PPROD)
+        return pprod_fp64(K, q, c);
+    else if (PROC == NOA_DCS_PROC_PHOTO)
+        return photo_fp64(K, q, c);
+    else
+        return ion_fp64(K, q, c);
+}
+
+template <int PROC>
+__device__ __forceinline__ bool i_open(double K, double q, const noa_dcs_consts &c) {
+    if (PROC == NOA_DCS_PROC_PPROD)
+        return pprod_live(K, q, c);
+    else if (PROC == NOA_DCS_PROC_PHOTO)
+        return photo_live(K, q, c);
+    else if (PROC == NOA_DCS_PROC_ION) {
+        // ionisation's early returns, dcs.hh:415-424
+        const double P2 = K * (K + 2. * c.mass);
+        const double Wmax = ion_wmax(P2, K + c.mass, c);
+        return !((Wmax < NOA_X_FRACTION * K) || (q > Wmax) || (q <= c.io_Wmin));
+    } else
+        return true;
+}
+
+// The closed-form ionisation integrals, dcs.hh:446-496 (FP64, IEEE order).
+__device__ __forceinline__ double ion_analytic(double K, double xlow, int moment, const noa_dcs_consts &c) {
+    const double mass = c.mass;
+    const double P2 = K * (K + 2. * mass);
+    const double E = K + mass;
+    const double Wmax = ion_wmax(P2, E, c);
+    if (Wmax < NOA_X_FRACTION * K)
+        return 0.;
+    double Wmin = c.io_Wmin;
+    const double qlow = K * xlow;
+    if (qlow >= Wmin)
+        Wmin = qlow;
+    if (Wmax <= Wmin)
+        return 0.;
+    const double a0 = x_div(0.5, P2), a1 = x_div(-1., Wmax), a2 = x_div(E * E, P2);
+    const double lw = log(x_div(Wmax, Wmin));
+    double term;
+    if (moment == 0)
+        term = x_add(x_add(x_mul(a0, Wmax - Wmin), x_mul(a1, lw)), x_mul(a2, x_sub(x_div(1., Wmin), x_div(1., Wmax))));
+    else
+        term = x_add(x_add(x_mul(x_mul(0.5, a0), x_sub(x_mul(Wmax, Wmax), x_mul(Wmin, Wmin))), x_mul(a1, Wmax - Wmin)),
+                     x_mul(a2, lw));
+    return x_mul(x_div(x_mul(1.535336E-05, c.Zd), c.A), term);
+}
+
+__device__ __forceinline__ int i_scan(int v, int *warp_tot, int *total) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    int x = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const int y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o)
+            x += y;
+    }
+    if (lane == 31)
+        warp_tot[warp] = x;
+    __syncthreads();
+    if (warp == 0) {
+        const int w = lane < (I_THREADS >> 5) ? warp_tot[lane] : 0;
+        int s = w;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int y = __shfl_up_sync(0xffffffffu, s, o);
+            if (lane >= o)
+                s += y;
+        }
+        if (lane < (I_THREADS >> 5))
+            warp_tot[lane] = s - w;
+        if (lane == 31)
+            *total = s;
+    }
+    __syncthreads();
+    return warp_tot[warp] + x - v;
+}
+
+// Weighted value of node slot (f h w of numerics.hh:86, f = dcs q or dcs q^2).
+template <int PROC>
+__device__ __forceinline__ double i_node_value(double K, double q, double h, int node, int moment,
+                                               const noa_dcs_consts &c) {
+    const double d = i_eval<PROC>(K, q, c);
+    const double f = moment == 0 ? x_mul(d, q) : x_mul(x_mul(d, q), q);
+    return x_mul(x_mul(f, h), kGL6W[node % 6]);
+}
+
+template <int PROC>
+__global__ void __launch_bounds__(I_THREADS) recoil_integral_kernel(const IntegralParams p, const noa_dcs_consts c) {
+    __shared__ double vals[I_PAIRS];   // weighted node values of the tile, [k][node]
+    __shared__ double qQ[I_QCAP];      // queued recoil energies
+    __shared__ int qS[I_QCAP];         // their slots in vals
+    __shared__ double sK[I_KMAX], sLb[I_KMAX], sH[I_KMAX];
+    __shared__ int warp_tot[I_THREADS / 32];
+    __shared__ int tile_open;
+    const int pairs = p.kpt * p.nodes;
+    const int64_t tiles = (p.n + p.kpt - 1) / p.kpt;
+    const double ion_thr = c.io_k_rad;  // 0.5 (m - me)^2 / me, dcs.hh:962-963
+
+    for (int64_t tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
+        const int64_t k0 = tile * p.kpt;
+        if ((int)threadIdx.x < p.kpt) {
+            // bounds of the t = log q rule for this K, numerics.hh:80-81
+            const int64_t ki = k0 + threadIdx.x;
+            const double K = ki < p.n ? p.K[ki] : 1.;
+            const double lb = log(K * p.xlow), ub = log(K);
+            sK[threadIdx.x] = K;
+            sLb[threadIdx.x] = lb;
+            sH[threadIdx.x] = x_div(ub - lb, (double)p.n_itv);
+        }
+        __syncthreads();
+        int qn = 0;
+        for (int base = 0; base < pairs; base += I_THREADS) {
+            const int slot = base + threadIdx.x;
+            bool open = false;
+            double q = 0.;
+            if (slot < pairs) {
+                const int kk = slot / p.nodes, i = slot - kk * p.nodes;
+                vals[slot] = 0.;
+                const double K = sK[kk];
+                if (k0 + kk < p.n && !(PROC == NOA_DCS_PROC_ION && K <= ion_thr)) {
+                    // node i of the composite rule, numerics.hh:84-86, in IEEE order
+                    const double t = x_add(sLb[kk], x_mul(sH[kk], (double)(i / 6) + kGL6X[i % 6]));
+                    q = lean_exp(t);
+                    open = i_open<PROC>(K, q, c);
+                }
+            }
+            int pos = qn + i_scan(open ? 1 : 0, warp_tot, &tile_open);
+            if (open) {
+                qQ[pos] = q;
+                qS[pos] = slot;
+            }
+            __syncthreads();
+            qn += tile_open;
+            while (qn >= I_THREADS) {
+                const int e = qn - I_THREADS + threadIdx.x;
+                const int sl = qS[e], kk = sl / p.nodes;
+                vals[sl] = i_node_value<PROC>(sK[kk], qQ[e], sH[kk], sl - kk * p.nodes, p.moment, c);
+                qn -= I_THREADS;
+                __syncthreads();
+            }
+        }
+        if ((int)threadIdx.x < qn) {
+            const int sl = qS[threadIdx.x], kk = sl / p.nodes;
+            vals[sl] = i_node_value<PROC>(sK[kk], qQ[threadIdx.x], sH[kk], sl - kk * p.nodes, p.moment, c);
+        }
+        __syncthreads();
+        // one thread per kinetic energy: node-ordered sum, as the reference
+        if ((int)threadIdx.x < p.kpt) {
+            const int64_t ki = k0 + threadIdx.x;
+            if (ki < p.n) {
+                const double K = sK[threadIdx.x];
+                double r;
+                if (PROC == NOA_DCS_PROC_ION && K <= ion_thr) {
+                    r = ion_analytic(K, p.xlow, p.moment, c);
+                } else {
+                    double s = 0.;
+                    const double *v = vals + threadIdx.x * p.nodes;
+                    for (int i = 0; i < p.nodes; i++)
+                        s = x_add(s, v[i]);
+                    r = x_div(s, K + c.mass);
+                }
+                p.out[ki] = r;
+            }
+        }
+        __syncthreads();
+    }
+}
+
+static int sm_count() {
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    return sms > 0 ? sms : 1;
+}
+
+} // namespace noa_dcs
+
+using namespace noa_dcs;
+
+cudaError_t noa_dcs_launch_recoil_integral(int process, int moment, const double *K, double *out, int64_t n,
+                                           double xlow, int min_points, const noa_dcs_consts *c,
+                                           cudaStream_t stream) {
+    if (n <= 0)
+        return cudaSuccess;
+    IntegralParams p;
+    p.K = K;
+    p.out = out;
+    p.n = n;
+    p.xlow = xlow;
+    p.n_itv = (min_points + 5) / 6;
+    p.nodes = 6 * p.n_itv;
+    if (p.nodes > I_PAIRS || p.nodes < 6)
+        return cudaErrorInvalidValue;
+    p.kpt = I_PAIRS / p.nodes;
+    if (p.kpt > I_KMAX)
+        p.kpt = I_KMAX;
+    p.moment = moment;
+    const int64_t tiles = (n + p.kpt - 1) / p.kpt;
+    const int64_t cap = (int64_t)sm_count() * 3;
+    const int grid = (int)(tiles < cap ? tiles : cap);
+    switch (process) {
+    case NOA_DCS_PROC_BREMS:
+        recoil_integral_kernel<NOA_DCS_PROC_BREMS><<<grid, I_THREADS, 0, stream>>>(p, *c);
+        break;
+    case NOA_DCS_PROC_PPROD:
+        recoil_integral_kernel<NOA_DCS_PROC_PPROD><<<grid, I_THREADS, 0, stream>>>(p, *c);
+        break;
+    case NOA_DCS_PROC_PHOTO:
+        recoil_integral_kernel<NOA_DCS_PROC_PHOTO><<<grid, I_THREADS, 0, stream>>>(p, *c);
+        break;
+    case NOA_DCS_PROC_ION:
+        recoil_integral_kernel<NOA_DCS_PROC_ION><<<grid, I_THREADS, 0, stream>>>(p, *c);
+        break;
+    default:
+        return cudaErrorInvalidValue;
+    }
+    return cudaGetLastError();
+}

@@ -37,3 +37,9 @@ cudaError_t noa_dcs_batched_launch32(int process, int threads, const void *param
 /* Resident CTAs per SM of one instantiation at the given dynamic smem. */
 int noa_dcs_batched_occupancy64(int process, int threads, size_t smem);
 int noa_dcs_batched_occupancy32(int process, int threads, size_t smem);
+
+/* Recoil integrals (dcs_integral.cu): moment 0 = DEL, 1 = CEL; min_points in
+ * 1..1536 (6 ceil(min_points / 6) nodes per K). */
+cudaError_t noa_dcs_launch_recoil_integral(int process, int moment, const double *K, double *out, int64_t n,
+                                           double xlow, int min_points, const noa_dcs_consts *c,
+                                           cudaStream_t stream);

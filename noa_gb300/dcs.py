@@ -15,10 +15,10 @@ misreads on those).
 import torch
 
 from . import _lib
-from .elements import MUON_MASS, STANDARD_ROCK, AtomicElement
+from .elements import MUON_MASS, STANDARD_ROCK, X_FRACTION, AtomicElement
 
 __all__ = [
-    "vmap", "map", "vmap_host",
+    "vmap", "map", "vmap_host", "recoil_integral",
     "vmap_bremsstrahlung", "vmap_pair_production", "vmap_photonuclear", "vmap_ionisation",
     "map_bremsstrahlung", "map_pair_production", "map_photonuclear", "map_ionisation",
 ]
@@ -85,6 +85,28 @@ def vmap_host(process, result, kinetic_energies, recoil_energies, element=STANDA
     _lib.check(lib.noa_dcs_vmap_host(_process_id(process), _lib.PRECISIONS[precision], result.data_ptr(),
                                      kinetic_energies.data_ptr(), recoil_energies.data_ptr(), n, el,
                                      float(mass)))
+    return result
+
+
+def recoil_integral(process, moment, result, kinetic_energies, xlow=X_FRACTION, element=STANDARD_ROCK,
+                    mass=MUON_MASS, min_points=180):
+    """GPU form of dcs::vmap_integral(dcs::recoil_integral(dcs::<process>,
+    del_integrand | cel_integrand)) (dcs.hh:89-130): result[i] = the DEL
+    (moment 0) or CEL (moment 1) integral for kinetic_energies[i]."""
+    lib = _lib.load()
+    _check_tensor(result, "result")
+    _check_tensor(kinetic_energies, "kinetic_energies", result.device)
+    n = result.numel()
+    if kinetic_energies.numel() != n:
+        raise RuntimeError("size mismatch")
+    if isinstance(moment, str):
+        moment = {"del": 0, "cel": 1}[moment.lower()]
+    el = _lib.element_struct(element)
+    with torch.cuda.device(result.device):
+        stream = torch.cuda.current_stream(result.device).cuda_stream
+        _lib.check(lib.noa_dcs_cuda_recoil_integral(_process_id(process), int(moment), result.data_ptr(),
+                                                    kinetic_energies.data_ptr(), n, float(xlow), el, float(mass),
+                                                    int(min_points), stream))
     return result
 
 
