@@ -55,6 +55,7 @@ def parse_args():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-batched", action="store_true")
+    ap.add_argument("--no-integrals", action="store_true")
     return ap.parse_args()
 
 
@@ -290,6 +291,46 @@ def time_batched(torch, args):
     return res
 
 
+def time_integrals(torch, args, with_cpu):
+    """DEL / CEL recoil integrals (dcs::vmap_integral(dcs::recoil_integral(...)),
+    xlow = 0.05, 180 nodes per K as in the reference's benchmark) over 1e5
+    seeded kinetic energies, FP64, per process and moment; the CPU oracle is
+    timed on the first 2000 energies with every host thread."""
+    from noa_gb300 import dcs
+    from noa_gb300.elements import MUON_MASS, STANDARD_ROCK, X_FRACTION
+    from noa_gb300.workload import kinetic_recoil
+    nk = 100_000
+    K, _ = kinetic_recoil(nk, offset=1 << 30)
+    tk = torch.from_numpy(K).cuda()
+    out = torch.empty_like(tk)
+    stream = torch.cuda.current_stream()
+    res = {"n_kinetic": nk, "nodes_per_K": 180, "xlow": X_FRACTION}
+    for p, name in enumerate(PROCESSES):
+        for moment, mname in ((0, "del"), (1, "cel")):
+            for _ in range(max(1, args.warmup)):
+                dcs.recoil_integral(p, moment, out, tk)
+            s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            steps = max(1, min(args.steps, 5))
+            torch.cuda.synchronize()
+            s.record(stream)
+            for _ in range(steps):
+                dcs.recoil_integral(p, moment, out, tk)
+            e.record(stream)
+            torch.cuda.synchronize()
+            t = s.elapsed_time(e) * 1e-3 / steps
+            entry = {"K_per_s": nk / t, "ms": 1e3 * t}
+            if with_cpu:
+                import oracle
+                ns = 2000
+                t0 = time.perf_counter()
+                oracle.recoil_integral(p, moment, K[:ns], X_FRACTION, STANDARD_ROCK, MUON_MASS, 180, threads=0)
+                tc = time.perf_counter() - t0
+                entry["cpu_port_K_per_s"] = ns / tc
+                entry["speedup_vs_cpu"] = entry["K_per_s"] / entry["cpu_port_K_per_s"]
+            res[f"{name}_{mname}"] = entry
+    return res
+
+
 def load_traffic():
     path = os.path.join(ROOT, "profiles", "traffic.json")
     try:
@@ -424,6 +465,8 @@ def run_ours(args):
     }
     if not args.no_batched:
         line["batched"] = time_batched(torch, args)
+    if not args.no_integrals:
+        line["recoil_integrals"] = time_integrals(torch, args, with_cpu=not args.no_cpu_baseline and world == 1)
     if not args.no_cpu_baseline and world == 1:
         cb = cpu_reference_rate(min(n, 1_000_000))
         line["cpu_baseline"] = {"value": cb["value"], "unit": "evals/s", "cores": cb["cores"], "kind": "port",
