@@ -169,6 +169,56 @@ int noa_dcs_cuda_vmap_batched_noalloc(int process, int precision, int n_segments
                                       const int64_t *counts, double mass, double *result, const double *K,
                                       const double *q, void *stream);
 
+/* ---- learned surrogate (no counterpart in the reference).  A
+ * 4 -> 128 -> 128 -> 128 -> 1 SiLU network predicts the residual of log DCS over
+ * an analytic baseline for pair production or photonuclear, from the features
+ * (log K, log nu, Z/100, log A).  Training runs on the GPU with the library's
+ * own BF16 tensor-core forward / backward kernels and Adam.  The parameter
+ * vector has NOA_DCS_MLP_NPARAM floats; norm holds 10 floats: feature shifts
+ * (4), feature scales (4), residual shift and scale. */
+#define NOA_DCS_MLP_NPARAM 33793
+typedef struct noa_dcs_mlp noa_dcs_mlp;
+
+int noa_dcs_mlp_create(noa_dcs_mlp **model, int process, int batch);
+int noa_dcs_mlp_set_params(noa_dcs_mlp *model, const float *params, const float *adam_m, const float *adam_v,
+                           int64_t step, const float *norm);
+int noa_dcs_mlp_get_params(noa_dcs_mlp *model, float *params, float *adam_m, float *adam_v, int64_t *step);
+/* Training data from the FP64 kernels: for pairs (K[i], q[i]) of element
+ * elements[elem[i]], raw features Xraw[i][4], residual R[i] = log DCS - baseline
+ * and valid[i] (0 where the DCS is zero).  Device buffers; synchronous. */
+int noa_dcs_mlp_prepare(int process, const double *K, const double *q, const uint8_t *elem, int64_t n,
+                        const noa_dcs_element *elements, int n_elements, double mass, float *Xraw, float *R,
+                        uint8_t *valid, void *stream);
+/* n_steps Adam steps on batches perm[b*batch .. (b+1)*batch) of the normalised
+ * data X[n][4], T[n]; cosine learning-rate decay from lr to lr_final;
+ * losses[n_steps] (device, optional) receives each batch's loss. */
+int noa_dcs_mlp_train(noa_dcs_mlp *model, const float *X, const float *T, int64_t n, const int32_t *perm,
+                      int64_t n_steps, float lr, float lr_final, float *losses, void *stream);
+/* Normalised network output for X[n][4] (device buffers). */
+int noa_dcs_mlp_predict(noa_dcs_mlp *model, const float *X, float *out, int64_t n, void *stream);
+/* Loss and gradient (NOA_DCS_MLP_NPARAM floats, device) of one batch of n rows. */
+int noa_dcs_mlp_gradient(noa_dcs_mlp *model, const float *X, const float *T, int n, float *grad, float *loss,
+                         void *stream);
+int noa_dcs_mlp_destroy(noa_dcs_mlp *model);
+const char *noa_dcs_mlp_last_error(void);
+/* Surrogate evaluation of n = sum(counts) pairs laid out as for a batch plan
+ * (segment s: element elements[s], counts[s] pairs; at most 16 segments,
+ * fewer than 2^31 pairs).  trust is the device trust grid
+ * uint8[n_segments][64][64] over (log K in [log 1e-3, log 1e6], log nu in
+ * [log 1e-7, 0]): pairs in a trusted cell are answered by the network
+ * (tcgen05 tensor cores), all others by the FP32C kernel (FP64 above
+ * `tolerance`).  Closed pairs get 0.  stats (pinned or host memory, optional)
+ * receives {network pairs, fallback pairs, status} when the stream reaches
+ * it; status NOA_DCS_ERROR_TIMEOUT reports an expired tensor-core wait.
+ * Allocates its pair lists on first use and when n grows. */
+int noa_dcs_mlp_infer(noa_dcs_mlp *model, const uint8_t *trust, int n_segments, const noa_dcs_element *elements,
+                      const int64_t *counts, double mass, double *result, const double *K, const double *q,
+                      float tolerance, unsigned long long *stats, void *stream);
+const char *noa_dcs_mlp_infer_last_error(void);
+/* Accessor used by the inference kernels of this library. */
+int noa_dcs_mlp_handles(noa_dcs_mlp *model, int *process, const float **params, const void **weights_bf16,
+                        const float **norm);
+
 /* Frees the host-path staging buffers of the current device (they are
  * otherwise kept for reuse until the process exits). */
 int noa_dcs_release_staging(void);

@@ -65,6 +65,18 @@ SIGNATURES = {
     "noa_dcs_batch_plan_execute_graph": (_INT, [_P, _P, _P, _P, _P]),
     "noa_dcs_batch_plan_destroy": (_INT, [_P]),
     "noa_dcs_batch_last_error": (ctypes.c_char_p, []),
+    "noa_dcs_mlp_create": (_INT, [ctypes.POINTER(_P), _INT, _INT]),
+    "noa_dcs_mlp_set_params": (_INT, [_P, _P, _P, _P, _I64, _P]),
+    "noa_dcs_mlp_get_params": (_INT, [_P, _P, _P, _P, ctypes.POINTER(_I64)]),
+    "noa_dcs_mlp_prepare": (_INT, [_INT, _P, _P, _P, _I64, _EP, _INT, _D, _P, _P, _P, _P]),
+    "noa_dcs_mlp_train": (_INT, [_P, _P, _P, _I64, _P, _I64, ctypes.c_float, ctypes.c_float, _P, _P]),
+    "noa_dcs_mlp_predict": (_INT, [_P, _P, _P, _I64, _P]),
+    "noa_dcs_mlp_gradient": (_INT, [_P, _P, _P, _INT, _P, _P, _P]),
+    "noa_dcs_mlp_destroy": (_INT, [_P]),
+    "noa_dcs_mlp_last_error": (ctypes.c_char_p, []),
+    "noa_dcs_mlp_infer": (_INT, [_P, _P, _INT, _EP, ctypes.POINTER(_I64), _D, _P, _P, _P, ctypes.c_float, _P, _P]),
+    "noa_dcs_mlp_infer_last_error": (ctypes.c_char_p, []),
+    "noa_dcs_mlp_handles": (_INT, [_P, _P, _P, _P, _P]),
     "noa_dcs_cuda_vmap_batched_noalloc": (_INT, [_INT, _INT, _INT, _EP, ctypes.POINTER(_I64), _D, _P, _P, _P, _P]),
 }
 

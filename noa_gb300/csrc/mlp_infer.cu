@@ -1,0 +1,517 @@
+/*
+ * Learned DCS surrogate, inference (noa_dcs_mlp_infer): three kernels on the
+ * caller's stream.
+ *
+ *  1. classify: per pair, the kinematic bounds decided as the FP64 kernels
+ *     decide them (closed -> 0), the float baseline of mlp.cuh, the
+ *     normalised features and the trust-grid cell.
+ *     Pairs inside the trained domain whose cell passed the held-out error
+ *     check go to the network list; the others to the fallback list (both in
+ *     the model's scratch, appended with warp-aggregated atomics).
+ *  2. network (tcgen05): a persistent CTA of two warpgroups evaluates tiles of
+ *     128 listed pairs.  Row r of a tile is TMEM lane r.  Layer 1 (4 -> 128)
+ *     and the output layer run in FP32 on the CUDA cores; the two 128 x 128
+ *     layers run on the 5th-generation tensor cores: the activations are
+ *     written to shared memory as BF16 hi / lo in the canonical no-swizzle
+ *     K-major layout, W2 and W3 (hi / lo, resident in shared memory for the
+ *     whole launch) are the B operands, and one thread issues
+ *     tcgen05.mma.cta_group::1.kind::f16 (M = N = 128, K = 16) for the three
+ *     products A_hi W_hi + A_lo W_hi + A_hi W_lo, accumulating in FP32 in TMEM.
+ *     tcgen05.commit signals an mbarrier; the epilogue reads the accumulator
+ *     with tcgen05.ld (warpgroup 0 columns 0-63, warpgroup 1 columns 64-127
+ *     of the same lanes), adds the bias and applies SiLU.
+ *     DCS = exp(baseline + residual), in float (1e-6 relative).
+ *  3. fallback: the FP32C evaluation (dcs_fp32c.cuh) of the fallback list,
+ *     with FP64 (dcs_fp64.cuh) for pairs above its tolerance.
+ *
+ * Every mbarrier wait is bounded; on expiry the kernel records
+ * NOA_DCS_ERROR_TIMEOUT in the model's status word, finishes its in-flight
+ * MMAs, frees its TMEM and returns.
+ */
+#include "dcs_fp32c.cuh"
+#include "dcs_fp64.cuh"
+#include "dcs_launch.h"
+#include "mlp.cuh"
+
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+#include <cstdio>
+
+using namespace noa_mlp;
+
+namespace {
+
+constexpr int NT = 256;                   // threads of the network kernel: 2 warpgroups
+constexpr int TILE = 128;                 // rows (pairs) per tile = TMEM lanes
+constexpr int MAT = H * H * 2;            // bytes of one 128 x 128 BF16 operand
+constexpr int SMEM_NET = 6 * MAT + 1024;  // W2 hi/lo, W3 hi/lo, A hi/lo, alignment slack
+constexpr int MAX_EL = 16;
+constexpr long long SPIN_LIMIT = 1LL << 26;
+
+struct InferParams {
+    const double *K;
+    const double *q;
+    double *out;
+    int n_seg;
+    int pad_;
+    int64_t seg_begin[MAX_EL + 1];
+    noa_dcs_consts consts[MAX_EL];
+    float logA[MAX_EL];
+    float Zf[MAX_EL];
+    Norm norm;
+    const uint8_t *trust;  // [n_seg][64][64]
+    float logk_lo, logk_span, lognu_lo, lognu_span;
+    // lists
+    int32_t *net_idx;
+    float *net_base;
+    float4 *net_feat;
+    int32_t *fb_idx;
+    uint8_t *fb_seg;
+    uint8_t *net_seg;
+    unsigned long long *counters;  // [0] network, [1] fallback, [2] status
+    float tol;
+};
+
+__device__ __forceinline__ void append(unsigned long long *counter, bool flag, int &slot) {
+    const unsigned m = __ballot_sync(0xffffffffu, flag);
+    const int lane = threadIdx.x & 31;
+    unsigned long long base = 0;
+    if (m && lane == __ffs(m) - 1)
+        base = atomicAdd(counter, (unsigned long long)__popc(m));
+    base = __shfl_sync(0xffffffffu, base, __ffs(m ? m : 1u) - 1);
+    slot = flag ? (int)(base + __popc(m & ((1u << lane) - 1u))) : -1;
+}
+
+template <int PROC>
+__global__ void __launch_bounds__(256) classify_kernel(const __grid_constant__ InferParams p) {
+    const int64_t n = p.seg_begin[p.n_seg];
+    for (int64_t base = (int64_t)blockIdx.x * blockDim.x; base < n; base += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t i = base + threadIdx.x;
+        bool to_net = false, to_fb = false;
+        int seg = 0;
+        float b = 0.f;
+        float4 f = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (i < n) {
+            while (seg + 1 < p.n_seg && i >= p.seg_begin[seg + 1])
+                seg++;
+            const noa_dcs_consts &c = p.consts[seg];
+            const double K = p.K[i], q = p.q[i];
+            float bf;
+            if (!baseline_fast<PROC>(K, q, c, bf)) {
+                p.out[i] = 0.;
+            } else {
+                const float lk = logf((float)K), ln = logf((float)q / (float)(K + c.mass));
+                const float fk = floorf((lk - p.logk_lo) / p.logk_span * 64.f);
+                const float fn = floorf((ln - p.lognu_lo) / p.lognu_span * 64.f);
+                bool trusted = false;
+                if (fk >= 0.f && fk < 64.f && fn >= 0.f && fn < 64.f && isfinite(bf))
+                    trusted = p.trust[(seg * 64 + (int)fk) * 64 + (int)fn] != 0;
+                if (trusted) {
+                    to_net = true;
+                    b = bf;
+                    f.x = (lk - p.norm.in_shift[0]) * p.norm.in_scale[0];
+                    f.y = (ln - p.norm.in_shift[1]) * p.norm.in_scale[1];
+                    f.z = (p.Zf[seg] * 0.01f - p.norm.in_shift[2]) * p.norm.in_scale[2];
+                    f.w = (p.logA[seg] - p.norm.in_shift[3]) * p.norm.in_scale[3];
+                } else {
+                    to_fb = true;
+                }
+            }
+        }
+        int s_net, s_fb;
+        append(&p.counters[0], to_net, s_net);
+        append(&p.counters[1], to_fb, s_fb);
+        if (to_net) {
+            p.net_idx[s_net] = (int32_t)i;
+            p.net_base[s_net] = b;
+            p.net_feat[s_net] = f;
+            p.net_seg[s_net] = (uint8_t)seg;
+        }
+        if (to_fb) {
+            p.fb_idx[s_fb] = (int32_t)i;
+            p.fb_seg[s_fb] = (uint8_t)seg;
+        }
+    }
+}
+
+template <int PROC>
+__global__ void __launch_bounds__(256) fallback_kernel(const __grid_constant__ InferParams p) {
+    const unsigned long long cnt = p.counters[1];
+    for (unsigned long long e = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x; e < cnt;
+         e += (unsigned long long)gridDim.x * blockDim.x) {
+        const int32_t i = p.fb_idx[e];
+        const noa_dcs_consts &c = p.consts[p.fb_seg[e]];
+        const double K = p.K[i], q = p.q[i];
+        float est;
+        double v = PROC == NOA_DCS_PAIR_PRODUCTION ? noa_dcs::pprod_fp32c<true>(K, q, c, est)
+                                                   : noa_dcs::photo_fp32c<true>(K, q, c, est);
+        if (!(est <= p.tol))
+            v = PROC == NOA_DCS_PAIR_PRODUCTION ? noa_dcs::pprod_fp64(K, q, c) : noa_dcs::photo_fp64(K, q, c);
+        p.out[i] = v;
+    }
+}
+
+// ---------------------------------------------------------------- tcgen05 helpers
+__device__ __forceinline__ uint32_t smem_u32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+// Offset of element (r, k) in a 128 x 128 BF16 operand in the canonical
+// K-major no-swizzle layout: 8 x 8 core matrices of 128 contiguous bytes,
+// K-adjacent core matrices 128 B apart (LBO), 8-row groups 2048 B apart (SBO).
+__device__ __forceinline__ uint32_t canon_off(int r, int k) {
+    return (uint32_t)((r >> 3) * 2048 + (k >> 3) * 128 + (r & 7) * 16 + (k & 7) * 2);
+}
+
+// Shared-memory matrix descriptor (tcgen05 format): start address, LBO and
+// SBO in units of 16 B, descriptor version 1 (bits 46-47), no swizzle.
+__device__ __forceinline__ uint64_t make_desc(uint32_t saddr) {
+    const uint64_t lbo = 128 >> 4, sbo = 2048 >> 4;
+    return (uint64_t)((saddr & 0x3FFFF) >> 4) | (lbo << 16) | (sbo << 32) | (1ULL << 46);
+}
+
+// Instruction descriptor, kind::f16: D FP32, A and B BF16, both K-major,
+// N = 128, M = 128.
+constexpr uint32_t IDESC = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(128 >> 3) << 17) |
+                           ((uint32_t)(128 >> 4) << 24);
+
+__device__ __forceinline__ void mma_f16(uint32_t d_tmem, uint64_t a, uint64_t b, uint32_t accumulate) {
+    asm volatile("{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+                 "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}"
+                 :
+                 : "r"(d_tmem), "l"(a), "l"(b), "r"(IDESC), "r"(accumulate));
+}
+
+__device__ __forceinline__ void mma_commit(uint32_t mbar) {
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(mbar)
+                 : "memory");
+}
+
+// Bounded wait for the mbarrier phase `parity`; false on expiry.
+__device__ __forceinline__ bool mbar_wait(uint32_t mbar, uint32_t parity) {
+    for (long long it = 0; it < SPIN_LIMIT; it++) {
+        uint32_t done;
+        asm volatile("{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+                     "selp.u32 %0, 1, 0, p;\n\t}"
+                     : "=r"(done)
+                     : "r"(mbar), "r"(parity)
+                     : "memory");
+        if (done)
+            return true;
+    }
+    return false;
+}
+
+__device__ __forceinline__ void tmem_ld32(uint32_t taddr, float (&v)[32]) {
+    uint32_t r[32];
+    asm volatile("tcgen05.ld.sync.aligned.32x32b.x32.b32 "
+                 "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
+                 "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+                   "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]),
+                   "=r"(r[14]), "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]),
+                   "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]),
+                   "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+                 : "r"(taddr));
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+    for (int i = 0; i < 32; i++)
+        v[i] = __uint_as_float(r[i]);
+}
+
+__device__ __forceinline__ void fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void fence_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+
+// Writes 8 consecutive activations (k .. k+7 of row r) as BF16 hi / lo.
+__device__ __forceinline__ void put8(unsigned char *Ahi, unsigned char *Alo, int r, int k, const float (&h)[8]) {
+    __nv_bfloat162 hi[4], lo[4];
+#pragma unroll
+    for (int i = 0; i < 4; i++) {
+        const __nv_bfloat16 a = __float2bfloat16_rn(h[2 * i]), b = __float2bfloat16_rn(h[2 * i + 1]);
+        hi[i] = __halves2bfloat162(a, b);
+        lo[i] = __halves2bfloat162(__float2bfloat16_rn(h[2 * i] - __bfloat162float(a)),
+                                   __float2bfloat16_rn(h[2 * i + 1] - __bfloat162float(b)));
+    }
+    const uint32_t o = canon_off(r, k);
+    *reinterpret_cast<uint4 *>(Ahi + o) = *reinterpret_cast<uint4 *>(hi);
+    *reinterpret_cast<uint4 *>(Alo + o) = *reinterpret_cast<uint4 *>(lo);
+}
+
+// Issues the 8 K-steps x 3 products of one 128 x 128 layer into TMEM column
+// offset dcol, and commits to the mbarrier.  One thread.
+__device__ __forceinline__ void issue_layer(uint32_t tmem, uint32_t dcol, uint32_t a_hi, uint32_t a_lo,
+                                            uint32_t w_hi, uint32_t w_lo, uint32_t mbar) {
+    fence_after();
+#pragma unroll
+    for (int ks = 0; ks < 8; ks++) {
+        const uint32_t o = ks * 256;  // two core matrices along K per step
+        mma_f16(tmem + dcol, make_desc(a_hi + o), make_desc(w_hi + o), ks > 0);
+        mma_f16(tmem + dcol, make_desc(a_lo + o), make_desc(w_hi + o), 1);
+        mma_f16(tmem + dcol, make_desc(a_hi + o), make_desc(w_lo + o), 1);
+    }
+    mma_commit(mbar);
+}
+
+template <int PROC>
+__global__ void __launch_bounds__(NT, 1) network_kernel(const __grid_constant__ InferParams p, const float *P,
+                                                        const __nv_bfloat16 *Wb) {
+    extern __shared__ unsigned char smem_raw[];
+    // 1024-byte aligned operand area
+    unsigned char *sm = smem_raw + ((1024 - (smem_u32(smem_raw) & 1023)) & 1023);
+    unsigned char *W2h = sm, *W2l = sm + MAT, *W3h = sm + 2 * MAT, *W3l = sm + 3 * MAT;
+    unsigned char *Ahi = sm + 4 * MAT, *Alo = sm + 5 * MAT;
+    __shared__ float sW1[H * IN], sb1[H], sb2[H], sb3[H], sWo[H];
+    __shared__ float spart[TILE];
+    __shared__ uint32_t tmem_slot;
+    __shared__ __align__(8) unsigned long long mbar;
+    __shared__ int s_abort;
+
+    const int tid = threadIdx.x, warp = tid >> 5;
+    const int row = tid & 127, half = tid >> 7;  // row = TMEM lane, half = column half
+    const unsigned long long cnt = p.counters[0];
+
+    // weights to shared memory (canonical layout) and registers / smem
+    for (int e = tid; e < H * H; e += NT) {
+        const int r = e / H, k = e % H;
+        const uint32_t o = canon_off(r, k);
+        *reinterpret_cast<__nv_bfloat16 *>(W2h + o) = Wb[e];
+        *reinterpret_cast<__nv_bfloat16 *>(W3h + o) = Wb[H * H + e];
+        *reinterpret_cast<__nv_bfloat16 *>(W2l + o) = Wb[2 * H * H + e];
+        *reinterpret_cast<__nv_bfloat16 *>(W3l + o) = Wb[3 * H * H + e];
+    }
+    for (int e = tid; e < H * IN; e += NT)
+        sW1[e] = P[OFF_W1 + e];
+    if (tid < H) {
+        sb1[tid] = P[OFF_B1 + tid];
+        sb2[tid] = P[OFF_B2 + tid];
+        sb3[tid] = P[OFF_B3 + tid];
+        sWo[tid] = P[OFF_WO + tid];
+    }
+    const float bo = P[OFF_BO];
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 256;" ::"r"(smem_u32(&tmem_slot)));
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+    }
+    if (tid == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&mbar)));
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        s_abort = 0;
+    }
+    fence_async_smem();
+    fence_before();
+    __syncthreads();
+    fence_after();
+    const uint32_t tmem = tmem_slot;
+    const uint32_t mb = smem_u32(&mbar);
+    const uint32_t a_hi = smem_u32(Ahi), a_lo = smem_u32(Alo);
+    const uint32_t lane_base = (uint32_t)((warp & 3) * 32) << 16;  // this warp's TMEM lane quarter
+    uint32_t phase = 0;
+
+    const long long tiles = (long long)((cnt + TILE - 1) / TILE);
+    for (long long t = blockIdx.x; t < tiles; t += gridDim.x) {
+        const long long e = t * TILE + row;
+        const bool valid = e < (long long)cnt;
+        float4 f = valid ? p.net_feat[e] : make_float4(0.f, 0.f, 0.f, 0.f);
+        // layer 1 (FP32): this thread's 64 hidden units of its row
+        for (int k0 = half * 64; k0 < half * 64 + 64; k0 += 8) {
+            float h[8];
+#pragma unroll
+            for (int j = 0; j < 8; j++) {
+                const int u = k0 + j;
+                float z = sb1[u];
+                z = fmaf(sW1[u * 4 + 0], f.x, z);
+                z = fmaf(sW1[u * 4 + 1], f.y, z);
+                z = fmaf(sW1[u * 4 + 2], f.z, z);
+                z = fmaf(sW1[u * 4 + 3], f.w, z);
+                h[j] = silu(z);
+            }
+            put8(Ahi, Alo, row, k0, h);
+        }
+        // layers 2 and 3 on the tensor cores
+        float y = 0.f;
+#pragma unroll 1
+        for (int layer = 0; layer < 2; layer++) {
+            fence_async_smem();
+            fence_before();
+            __syncthreads();
+            if (tid == 0)
+                issue_layer(tmem, layer * 128, a_hi, a_lo, smem_u32(layer ? W3h : W2h), smem_u32(layer ? W3l : W2l),
+                            mb);
+            const bool ok = mbar_wait(mb, phase);
+            phase ^= 1u;
+            if (!ok)
+                s_abort = 1;
+            fence_after();
+            __syncthreads();
+            if (s_abort)
+                break;
+            const float *bias = layer ? sb3 : sb2;
+#pragma unroll 1
+            for (int c0 = half * 64; c0 < half * 64 + 64; c0 += 32) {
+                float v[32];
+                tmem_ld32(tmem + lane_base + layer * 128 + c0, v);
+                if (layer == 0) {
+#pragma unroll
+                    for (int g = 0; g < 4; g++) {
+                        float h[8];
+#pragma unroll
+                        for (int j = 0; j < 8; j++)
+                            h[j] = silu(v[g * 8 + j] + bias[c0 + g * 8 + j]);
+                        put8(Ahi, Alo, row, c0 + g * 8, h);
+                    }
+                } else {
+#pragma unroll
+                    for (int j = 0; j < 32; j++)
+                        y = fmaf(sWo[c0 + j], silu(v[j] + bias[c0 + j]), y);
+                }
+            }
+        }
+        if (s_abort)
+            break;
+        // output: sum the two halves, DCS = exp(baseline + residual)
+        if (half == 1)
+            spart[row] = y;
+        fence_before();
+        __syncthreads();
+        if (half == 0 && valid) {
+            const float yy = y + spart[row] + bo;
+            const float r = p.norm.out_shift + yy / p.norm.out_scale;
+            p.out[p.net_idx[e]] = (double)expf(p.net_base[e] + r);
+        }
+    }
+    if (s_abort && tid == 0)
+        atomicMax(&p.counters[2], (unsigned long long)NOA_DCS_ERROR_TIMEOUT);
+    fence_before();
+    __syncthreads();
+    fence_after();
+    if (warp == 0)
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 256;" ::"r"(tmem));
+}
+
+} // namespace
+
+// ---------------------------------------------------------------- C ABI
+struct noa_dcs_mlp;  // defined in mlp_train.cu
+extern "C" int noa_dcs_mlp_handles(noa_dcs_mlp *m, int *process, const float **P, const void **Wb,
+                                   const float **norm);
+
+namespace {
+
+struct InferScratch {
+    int device = -1;
+    int64_t cap = 0;
+    void *buf = nullptr;
+};
+InferScratch g_scratch;  // grown on demand; one per process (the inference call is not thread-safe)
+thread_local char g_ierr[256] = "";
+
+int ifail(int st, const char *msg, cudaError_t e = cudaSuccess) {
+    if (e != cudaSuccess)
+        snprintf(g_ierr, sizeof g_ierr, "%s: %s", msg, cudaGetErrorString(e));
+    else
+        snprintf(g_ierr, sizeof g_ierr, "%s", msg);
+    return st;
+}
+
+} // namespace
+
+extern "C" int noa_dcs_mlp_infer(noa_dcs_mlp *model, const uint8_t *trust, int n_seg, const noa_dcs_element *elements,
+                                 const int64_t *counts, double mass, double *result, const double *K, const double *q,
+                                 float tolerance, unsigned long long *stats, void *stream) {
+    g_ierr[0] = '\0';
+    int process = 0;
+    const float *P = nullptr, *norm = nullptr;
+    const void *Wb = nullptr;
+    if (!model || noa_dcs_mlp_handles(model, &process, &P, &Wb, &norm))
+        return ifail(NOA_DCS_ERROR_INVALID_VALUE, "invalid model");
+    if (n_seg < 1 || n_seg > MAX_EL || !elements || !counts || !trust)
+        return ifail(NOA_DCS_ERROR_INVALID_VALUE, "segments must number 1..16, with a trust grid");
+    if (!(tolerance > 0.f && tolerance < 1.f))
+        return ifail(NOA_DCS_ERROR_INVALID_VALUE, "fallback tolerance must lie in (0, 1)");
+    InferParams p;
+    memset(&p, 0, sizeof p);
+    p.K = K;
+    p.q = q;
+    p.out = result;
+    p.n_seg = n_seg;
+    for (int s = 0; s < n_seg; s++) {
+        if (counts[s] < 0)
+            return ifail(NOA_DCS_ERROR_INVALID_VALUE, "negative count");
+        p.seg_begin[s + 1] = p.seg_begin[s] + counts[s];
+        noa_dcs_fill_consts(&p.consts[s], elements[s].A, elements[s].I, elements[s].Z, mass);
+        p.logA[s] = (float)log(elements[s].A);
+        p.Zf[s] = (float)elements[s].Z;
+    }
+    const int64_t n = p.seg_begin[n_seg];
+    if (n >= (1LL << 31))
+        return ifail(NOA_DCS_ERROR_INVALID_VALUE, "at most 2^31 - 1 pairs per call");
+    if (n == 0)
+        return NOA_DCS_SUCCESS;
+    memcpy(&p.norm, norm, sizeof p.norm);
+    p.trust = trust;
+    p.logk_lo = (float)log(1e-3);
+    p.logk_span = (float)(log(1e6) - log(1e-3));
+    p.lognu_lo = (float)log(1e-7);
+    p.lognu_span = (float)(0.0 - log(1e-7));
+    p.tol = tolerance;
+    // scratch: counters, then the two lists
+    int dev = 0;
+    cudaGetDevice(&dev);
+    const size_t per = sizeof(int32_t) + sizeof(float) + sizeof(float4) + 1 + sizeof(int32_t) + 1;
+    if (g_scratch.device != dev || g_scratch.cap < n) {
+        if (g_scratch.buf)
+            cudaFree(g_scratch.buf);
+        g_scratch.buf = nullptr;
+        const cudaError_t e = cudaMalloc(&g_scratch.buf, 64 + per * (size_t)n + 64);
+        if (e != cudaSuccess) {
+            g_scratch.cap = 0;
+            return ifail(NOA_DCS_ERROR_CUDA, "cudaMalloc(inference lists)", e);
+        }
+        g_scratch.cap = n;
+        g_scratch.device = dev;
+    }
+    unsigned char *b = static_cast<unsigned char *>(g_scratch.buf);
+    p.counters = reinterpret_cast<unsigned long long *>(b);
+    p.net_feat = reinterpret_cast<float4 *>(b + 64);
+    p.net_idx = reinterpret_cast<int32_t *>(p.net_feat + n);
+    p.net_base = reinterpret_cast<float *>(p.net_idx + n);
+    p.fb_idx = reinterpret_cast<int32_t *>(p.net_base + n);
+    p.net_seg = reinterpret_cast<uint8_t *>(p.fb_idx + n);
+    p.fb_seg = p.net_seg + n;
+    cudaStream_t s = (cudaStream_t)stream;
+    cudaError_t e = cudaMemsetAsync(p.counters, 0, 64, s);
+    int sms = 1;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const int64_t blocks = (n + 255) / 256;
+    const int cgrid = (int)(blocks < sms * 8 ? blocks : sms * 8);
+    if (e == cudaSuccess) {
+        if (process == NOA_DCS_PAIR_PRODUCTION)
+            classify_kernel<NOA_DCS_PAIR_PRODUCTION><<<cgrid, 256, 0, s>>>(p);
+        else
+            classify_kernel<NOA_DCS_PHOTONUCLEAR><<<cgrid, 256, 0, s>>>(p);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) {
+        auto k = process == NOA_DCS_PAIR_PRODUCTION ? network_kernel<NOA_DCS_PAIR_PRODUCTION>
+                                                    : network_kernel<NOA_DCS_PHOTONUCLEAR>;
+        e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_NET);
+        if (e == cudaSuccess) {
+            k<<<sms, NT, SMEM_NET, s>>>(p, P, static_cast<const __nv_bfloat16 *>(Wb));
+            e = cudaGetLastError();
+        }
+    }
+    if (e == cudaSuccess) {
+        if (process == NOA_DCS_PAIR_PRODUCTION)
+            fallback_kernel<NOA_DCS_PAIR_PRODUCTION><<<sms * 8, 256, 0, s>>>(p);
+        else
+            fallback_kernel<NOA_DCS_PHOTONUCLEAR><<<sms * 8, 256, 0, s>>>(p);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess && stats)
+        e = cudaMemcpyAsync(stats, p.counters, 3 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, s);
+    if (e != cudaSuccess)
+        return ifail(NOA_DCS_ERROR_CUDA, "inference launch", e);
+    return NOA_DCS_SUCCESS;
+}
+
+extern "C" const char *noa_dcs_mlp_infer_last_error(void) { return g_ierr; }

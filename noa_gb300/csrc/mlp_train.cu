@@ -1,0 +1,660 @@
+/*
+ * Learned DCS surrogate: training-data preparation, forward / backward / Adam
+ * kernels and the C ABI of the model object (include/noa_dcs.h,
+ * noa_dcs_mlp_*).  No counterpart in the reference.
+ *
+ * Training runs on the tensor cores in BF16 with FP32 accumulation
+ * (mma.sync m16n8k16): the 128 x 128 products of the two hidden layers, their
+ * input gradients and their weight gradients.  The first layer (4 inputs) and
+ * the output layer (1 output) are FP32 on the CUDA cores.  In the forward
+ * products both the hidden activations and the weights enter as a BF16 hi +
+ * lo pair (x = hi + lo, 16 significant bits), as three products
+ * A_hi W_hi + A_lo W_hi + A_hi W_lo with FP32 accumulation; the weight pairs
+ * are refreshed from the FP32 master copy after every Adam step, so training
+ * sees the numerics of inference.  Gradients flow in single BF16.
+ *
+ * Loss: mean squared error of the normalised residual (mlp.cuh).
+ */
+#include "dcs_fp64.cuh"
+#include "dcs_launch.h"
+#include "mlp.cuh"
+
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <new>
+
+using namespace noa_mlp;
+
+namespace {
+
+constexpr int LD = H + 8;  // padded bf16 row of a 128-wide smem tile (ldmatrix without bank conflicts)
+constexpr int G_THREADS = 256;
+constexpr size_t G_SMEM = 4u * H * LD * sizeof(__nv_bfloat16);
+
+enum { G_FWD = 0, G_DX = 1, G_DW = 2 };
+
+__device__ __forceinline__ void ldsm_x4(unsigned &r0, unsigned &r1, unsigned &r2, unsigned &r3, const void *p) {
+    const unsigned a = (unsigned)__cvta_generic_to_shared(p);
+    asm volatile("ldmatrix.sync.aligned.m8n8.x4.shared.b16 {%0,%1,%2,%3}, [%4];"
+                 : "=r"(r0), "=r"(r1), "=r"(r2), "=r"(r3)
+                 : "r"(a));
+}
+__device__ __forceinline__ void ldsm_x4_t(unsigned &r0, unsigned &r1, unsigned &r2, unsigned &r3, const void *p) {
+    const unsigned a = (unsigned)__cvta_generic_to_shared(p);
+    asm volatile("ldmatrix.sync.aligned.m8n8.x4.trans.shared.b16 {%0,%1,%2,%3}, [%4];"
+                 : "=r"(r0), "=r"(r1), "=r"(r2), "=r"(r3)
+                 : "r"(a));
+}
+__device__ __forceinline__ void mma_bf16(float (&d)[4], const unsigned (&a)[4], unsigned b0, unsigned b1) {
+    asm volatile("mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+                 "{%0,%1,%2,%3};"
+                 : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
+                 : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
+}
+
+struct GemmArgs {
+    const float *A;        // FWD: layer input H [M][128]; DX, DW: dZ [M][128]
+    const float *B;        // DW: H_prev [M][128]
+    const __nv_bfloat16 *W; // FWD, DX: weights [128 out][128 in] (hi); FWD also reads lo at W + 2*128*128
+    const float *bias;     // FWD
+    const float *zprev;    // DX: pre-activation of the previous layer [M][128]
+    float *outZ;           // FWD: Z; DX: dZ_prev
+    float *outH;           // FWD: H = silu(Z)
+    float *dW;             // DW: [128 out][128 in], accumulated
+    float *db;             // DW: [128], accumulated
+    int M;
+};
+
+// One CTA, 8 warps, a 128 x 128 output tile; warp w owns rows 16w..16w+15.
+//   FWD: Z = A W^T + b (A split hi/lo), H = silu(Z)
+//   DX : dZ_prev = (dZ W) * silu'(z_prev)
+//   DW : dW += dZ^T H_prev over this CTA's 128 samples, db += sum dZ
+template <int MODE>
+__global__ void __launch_bounds__(G_THREADS) mlp_gemm_kernel(const GemmArgs g) {
+    extern __shared__ __align__(16) unsigned char sm[];
+    __nv_bfloat16 *sA = reinterpret_cast<__nv_bfloat16 *>(sm);
+    __nv_bfloat16 *sAl = sA + H * LD;
+    __nv_bfloat16 *sB = sAl + H * LD;
+    __nv_bfloat16 *sBl = sB + H * LD;
+    const int row0 = blockIdx.x * H;
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+
+    // stage operands (FP32 -> BF16; FWD keeps the rounding residue as lo)
+    for (int e = tid; e < H * H; e += G_THREADS) {
+        const int r = e / H, c = e % H;
+        const bool in = row0 + r < g.M;
+        const float a = in ? g.A[(size_t)(row0 + r) * H + c] : 0.f;
+        const __nv_bfloat16 ah = __float2bfloat16_rn(a);
+        sA[r * LD + c] = ah;
+        if (MODE == G_FWD)
+            sAl[r * LD + c] = __float2bfloat16_rn(a - __bfloat162float(ah));
+        if (MODE == G_DW)
+            sB[r * LD + c] = __float2bfloat16_rn(in ? g.B[(size_t)(row0 + r) * H + c] : 0.f);
+        else
+            sB[r * LD + c] = g.W[r * H + c];
+        if (MODE == G_FWD)
+            sBl[r * LD + c] = g.W[2 * H * H + r * H + c];
+    }
+    __syncthreads();
+
+    float acc[16][4];
+#pragma unroll
+    for (int i = 0; i < 16; i++)
+        acc[i][0] = acc[i][1] = acc[i][2] = acc[i][3] = 0.f;
+    const int mi = lane >> 3, mr = lane & 7;  // which 8x8 matrix this lane addresses, and its row
+#pragma unroll 1
+    for (int ks = 0; ks < H / 16; ks++) {
+        const int k0 = ks * 16;
+        unsigned a[4], al[4];
+        if (MODE == G_DW) {
+            // A_op[m][k] = dZ[k][m]: transposed loads of the stored [k][m] tile
+            const int kr = k0 + (mi >> 1) * 8 + mr, mc = warp * 16 + (mi & 1) * 8;
+            ldsm_x4_t(a[0], a[1], a[2], a[3], sA + kr * LD + mc);
+        } else {
+            const int r = warp * 16 + (mi & 1) * 8 + mr, c = k0 + (mi >> 1) * 8;
+            ldsm_x4(a[0], a[1], a[2], a[3], sA + r * LD + c);
+            if (MODE == G_FWD)
+                ldsm_x4(al[0], al[1], al[2], al[3], sAl + r * LD + c);
+        }
+#pragma unroll
+        for (int nb = 0; nb < 16; nb += 2) {
+            unsigned b0, b1, b2, b3, l0 = 0, l1 = 0, l2 = 0, l3 = 0;
+            if (MODE == G_FWD) {
+                // B_op[k][n] = W[n][k]: rows n of W, k contiguous
+                const int n = nb * 8 + (mi >> 1) * 8 + mr, c = k0 + (mi & 1) * 8;
+                ldsm_x4(b0, b1, b2, b3, sB + n * LD + c);
+                ldsm_x4(l0, l1, l2, l3, sBl + n * LD + c);
+            } else {
+                // B_op[k][n] stored [k][n] (DX: W[out][in]; DW: H_prev[sample][in]): transposed loads
+                const int k = k0 + (mi & 1) * 8 + mr, c = nb * 8 + (mi >> 1) * 8;
+                ldsm_x4_t(b0, b1, b2, b3, sB + k * LD + c);
+            }
+            mma_bf16(acc[nb], a, b0, b1);
+            mma_bf16(acc[nb + 1], a, b2, b3);
+            if (MODE == G_FWD) {
+                mma_bf16(acc[nb], al, b0, b1);
+                mma_bf16(acc[nb + 1], al, b2, b3);
+                mma_bf16(acc[nb], a, l0, l1);
+                mma_bf16(acc[nb + 1], a, l2, l3);
+            }
+        }
+    }
+
+    // epilogue: acc[nb] = rows (r, r+8), cols (c, c+1)
+    const int r = warp * 16 + (lane >> 2), cq = (lane & 3) * 2;
+#pragma unroll
+    for (int nb = 0; nb < 16; nb++) {
+#pragma unroll
+        for (int h = 0; h < 2; h++) {
+            const int rr = r + h * 8;
+#pragma unroll
+            for (int j = 0; j < 2; j++) {
+                const int cc = nb * 8 + cq + j;
+                const float v = acc[nb][h * 2 + j];
+                if (MODE == G_DW) {
+                    atomicAdd(&g.dW[rr * H + cc], v);
+                } else if (row0 + rr < g.M) {
+                    const size_t o = (size_t)(row0 + rr) * H + cc;
+                    if (MODE == G_FWD) {
+                        const float z = v + g.bias[cc];
+                        g.outZ[o] = z;
+                        g.outH[o] = silu(z);
+                    } else {
+                        g.outZ[o] = v * dsilu(g.zprev[o]);
+                    }
+                }
+            }
+        }
+    }
+    if (MODE == G_DW && tid < H) {
+        float s = 0.f;
+        for (int k = 0; k < H && row0 + k < g.M; k++)
+            s += g.A[(size_t)(row0 + k) * H + tid];
+        atomicAdd(&g.db[tid], s);
+    }
+}
+
+// Layer 1 (FP32): Z1 = X W1^T + b1, H1 = silu(Z1).
+__global__ void mlp_fwd1_kernel(const float *__restrict__ X, const float *__restrict__ P, float *Z1, float *H1,
+                                int M) {
+    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < M * H; e += gridDim.x * blockDim.x) {
+        const int s = e / H, j = e % H;
+        float z = P[OFF_B1 + j];
+#pragma unroll
+        for (int i = 0; i < IN; i++)
+            z = fmaf(P[OFF_W1 + j * IN + i], X[s * IN + i], z);
+        Z1[e] = z;
+        H1[e] = silu(z);
+    }
+}
+
+// Output layer (FP32) and the loss gradient: pred = Wo h3 + bo,
+// loss = mean (pred - t)^2 over the batch of M samples (scaled by inv_batch);
+// dZ3 = dpred Wo * silu'(z3); dWo, dbo accumulated per CTA.  128 samples per CTA.
+__global__ void __launch_bounds__(128) mlp_out_kernel(const float *__restrict__ H3, const float *__restrict__ Z3,
+                                                      const float *__restrict__ T, const float *__restrict__ P,
+                                                      float *dZ3, float *G, float *loss, int M, float inv_batch,
+                                                      float *pred_out) {
+    __shared__ float sd[128];
+    const int s = blockIdx.x * 128 + threadIdx.x;
+    float dp = 0.f;
+    if (s < M) {
+        float y = P[OFF_BO];
+        for (int k = 0; k < H; k++)
+            y = fmaf(P[OFF_WO + k], H3[(size_t)s * H + k], y);
+        if (pred_out)
+            pred_out[s] = y;
+        if (T) {
+            const float d = y - T[s];
+            dp = 2.f * d * inv_batch;
+            atomicAdd(loss, d * d * inv_batch);
+        }
+    }
+    sd[threadIdx.x] = dp;
+    __syncthreads();
+    if (!T)
+        return;
+    if (s < M)
+        for (int k = 0; k < H; k++)
+            dZ3[(size_t)s * H + k] = dp * P[OFF_WO + k] * dsilu(Z3[(size_t)s * H + k]);
+    // dWo[k] = sum_s dp_s h3[s][k], thread k
+    const int k = threadIdx.x;
+    float g = 0.f;
+    for (int i = 0; i < 128 && blockIdx.x * 128 + i < M; i++)
+        g = fmaf(sd[i], H3[(size_t)(blockIdx.x * 128 + i) * H + k], g);
+    atomicAdd(&G[OFF_WO + k], g);
+    if (k == 0) {
+        float b = 0.f;
+        for (int i = 0; i < 128; i++)
+            b += sd[i];
+        atomicAdd(&G[OFF_BO], b);
+    }
+}
+
+// Layer-1 gradients: dW1[j][i] += sum_s dZ1[s][j] X[s][i], db1 += sum dZ1.  128 samples per CTA.
+__global__ void __launch_bounds__(128) mlp_bwd1_kernel(const float *__restrict__ dZ1, const float *__restrict__ X,
+                                                       float *G, int M) {
+    const int j = threadIdx.x;
+    float gw[IN] = {0.f, 0.f, 0.f, 0.f}, gb = 0.f;
+    for (int i = 0; i < 128; i++) {
+        const int s = blockIdx.x * 128 + i;
+        if (s >= M)
+            break;
+        const float d = dZ1[(size_t)s * H + j];
+        gb += d;
+#pragma unroll
+        for (int c = 0; c < IN; c++)
+            gw[c] = fmaf(d, X[s * IN + c], gw[c]);
+    }
+#pragma unroll
+    for (int c = 0; c < IN; c++)
+        atomicAdd(&G[OFF_W1 + j * IN + c], gw[c]);
+    atomicAdd(&G[OFF_B1 + j], gb);
+}
+
+// Adam (Kingma & Ba 2015) on the FP32 master parameters; refreshes the BF16
+// copies of W2, W3 used by the tensor-core products.
+__global__ void mlp_adam_kernel(float *P, const float *G, float *Mm, float *V, __nv_bfloat16 *Wb, float lr,
+                                float b1, float b2, float eps, float c1, float c2) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < NPARAM; i += gridDim.x * blockDim.x) {
+        const float g = G[i];
+        const float m = b1 * Mm[i] + (1.f - b1) * g;
+        const float v = b2 * V[i] + (1.f - b2) * g * g;
+        Mm[i] = m;
+        V[i] = v;
+        const float p = P[i] - lr * (m * c1) / (sqrtf(v * c2) + eps);
+        P[i] = p;
+        int w = -1;
+        if (i >= OFF_W2 && i < OFF_W2 + H * H)
+            w = i - OFF_W2;
+        else if (i >= OFF_W3 && i < OFF_W3 + H * H)
+            w = H * H + i - OFF_W3;
+        if (w >= 0) {
+            const __nv_bfloat16 hi = __float2bfloat16_rn(p);
+            Wb[w] = hi;
+            Wb[2 * H * H + w] = __float2bfloat16_rn(p - __bfloat162float(hi));
+        }
+    }
+}
+
+// BF16 hi / lo pairs of W2, W3: Wb[0 .. 2HH) hi (W2 then W3), Wb[2HH .. 4HH) lo.
+__global__ void mlp_round_weights_kernel(const float *P, __nv_bfloat16 *Wb) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < 2 * H * H; i += gridDim.x * blockDim.x) {
+        const float p = i < H * H ? P[OFF_W2 + i] : P[OFF_W3 + i - H * H];
+        const __nv_bfloat16 hi = __float2bfloat16_rn(p);
+        Wb[i] = hi;
+        Wb[2 * H * H + i] = __float2bfloat16_rn(p - __bfloat162float(hi));
+    }
+}
+
+// Gathers a batch: Xb[i] = X[perm[i]], Tb[i] = T[perm[i]].
+__global__ void mlp_gather_kernel(const float *X, const float *T, const int32_t *perm, float *Xb, float *Tb, int M) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < M; i += gridDim.x * blockDim.x) {
+        const int s = perm[i];
+#pragma unroll
+        for (int c = 0; c < IN; c++)
+            Xb[i * IN + c] = X[(size_t)s * IN + c];
+        if (T)
+            Tb[i] = T[s];
+    }
+}
+
+// Training data: raw features and the residual target from the FP64 plain
+// kernels (dcs_fp64.cuh).  valid = 0 for closed pairs (DCS = 0) and pairs
+// whose DCS underflows the baseline's log.
+template <int PROC>
+__global__ void mlp_prepare_kernel(const double *K, const double *q, const uint8_t *elem, int64_t n,
+                                   const noa_dcs_consts *consts, const float *logA, float *Xraw, float *R,
+                                   uint8_t *valid) {
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const noa_dcs_consts &c = consts[elem[i]];
+        double base;
+        bool ok = baseline<PROC>(K[i], q[i], c, base);
+        double d = 0.;
+        if (ok) {
+            d = PROC == NOA_DCS_PAIR_PRODUCTION ? noa_dcs::pprod_fp64(K[i], q[i], c) : noa_dcs::photo_fp64(K[i], q[i], c);
+            ok = d > 0. && isfinite(base);
+        }
+        const double nu = q[i] / (K[i] + c.mass);
+        Xraw[i * IN + 0] = (float)log(K[i]);
+        Xraw[i * IN + 1] = (float)log(nu);
+        Xraw[i * IN + 2] = (float)c.Zd * 0.01f;
+        Xraw[i * IN + 3] = logA[elem[i]];
+        R[i] = ok ? (float)(log(d) - base) : 0.f;
+        valid[i] = ok ? 1 : 0;
+    }
+}
+
+} // namespace
+
+struct noa_dcs_mlp {
+    int process = 0;
+    int batch = 0;
+    float *P = nullptr, *G = nullptr, *Mm = nullptr, *V = nullptr;
+    __nv_bfloat16 *Wb = nullptr;
+    float *Xb = nullptr, *Tb = nullptr;
+    float *Z1 = nullptr, *H1 = nullptr, *Z2 = nullptr, *H2 = nullptr, *Z3 = nullptr, *H3 = nullptr;
+    float *D3 = nullptr, *D2 = nullptr, *D1 = nullptr;
+    float *loss = nullptr;
+    int64_t step = 0;
+    float norm[2 * IN + 2] = {};
+};
+
+namespace {
+
+thread_local char g_merr[256] = "";
+
+int mfail(int st, const char *msg, cudaError_t e = cudaSuccess) {
+    if (e != cudaSuccess)
+        snprintf(g_merr, sizeof g_merr, "%s: %s", msg, cudaGetErrorString(e));
+    else
+        snprintf(g_merr, sizeof g_merr, "%s", msg);
+    return st;
+}
+
+cudaError_t set_gemm_smem() {
+    static bool done = false;
+    if (done)
+        return cudaSuccess;
+    cudaError_t e = cudaFuncSetAttribute(mlp_gemm_kernel<G_FWD>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)G_SMEM);
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(mlp_gemm_kernel<G_DX>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)G_SMEM);
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(mlp_gemm_kernel<G_DW>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)G_SMEM);
+    done = e == cudaSuccess;
+    return e;
+}
+
+// Forward over M <= batch rows already in m->Xb; prediction to pred if given.
+cudaError_t forward(noa_dcs_mlp *m, int M, float *pred, cudaStream_t s) {
+    const int tiles = (M + H - 1) / H;
+    mlp_fwd1_kernel<<<(M * H + 255) / 256, 256, 0, s>>>(m->Xb, m->P, m->Z1, m->H1, M);
+    GemmArgs g{};
+    g.M = M;
+    g.A = m->H1;
+    g.W = m->Wb;
+    g.bias = m->P + OFF_B2;
+    g.outZ = m->Z2;
+    g.outH = m->H2;
+    mlp_gemm_kernel<G_FWD><<<tiles, G_THREADS, G_SMEM, s>>>(g);
+    g.A = m->H2;
+    g.W = m->Wb + H * H;
+    g.bias = m->P + OFF_B3;
+    g.outZ = m->Z3;
+    g.outH = m->H3;
+    mlp_gemm_kernel<G_FWD><<<tiles, G_THREADS, G_SMEM, s>>>(g);
+    if (pred)
+        mlp_out_kernel<<<tiles, 128, 0, s>>>(m->H3, m->Z3, nullptr, m->P, nullptr, nullptr, nullptr, M, 0.f, pred);
+    return cudaGetLastError();
+}
+
+// Loss and gradient of one batch of M rows in Xb / Tb into m->G (zeroed first).
+cudaError_t backward(noa_dcs_mlp *m, int M, cudaStream_t s) {
+    const int tiles = (M + H - 1) / H;
+    cudaError_t e = cudaMemsetAsync(m->G, 0, sizeof(float) * NPARAM, s);
+    if (e != cudaSuccess)
+        return e;
+    if ((e = forward(m, M, nullptr, s)) != cudaSuccess)
+        return e;
+    mlp_out_kernel<<<tiles, 128, 0, s>>>(m->H3, m->Z3, m->Tb, m->P, m->D3, m->G, m->loss, M, 1.f / (float)M,
+                                         nullptr);
+    GemmArgs g{};
+    g.M = M;
+    // layer 3: dW3 = dZ3^T H2, dZ2 = (dZ3 W3) silu'(Z2)
+    g.A = m->D3;
+    g.B = m->H2;
+    g.dW = m->G + OFF_W3;
+    g.db = m->G + OFF_B3;
+    mlp_gemm_kernel<G_DW><<<tiles, G_THREADS, G_SMEM, s>>>(g);
+    g.W = m->Wb + H * H;
+    g.zprev = m->Z2;
+    g.outZ = m->D2;
+    mlp_gemm_kernel<G_DX><<<tiles, G_THREADS, G_SMEM, s>>>(g);
+    // layer 2: dW2 = dZ2^T H1, dZ1 = (dZ2 W2) silu'(Z1)
+    g.A = m->D2;
+    g.B = m->H1;
+    g.dW = m->G + OFF_W2;
+    g.db = m->G + OFF_B2;
+    mlp_gemm_kernel<G_DW><<<tiles, G_THREADS, G_SMEM, s>>>(g);
+    g.W = m->Wb;
+    g.zprev = m->Z1;
+    g.outZ = m->D1;
+    mlp_gemm_kernel<G_DX><<<tiles, G_THREADS, G_SMEM, s>>>(g);
+    mlp_bwd1_kernel<<<tiles, 128, 0, s>>>(m->D1, m->Xb, m->G, M);
+    return cudaGetLastError();
+}
+
+} // namespace
+
+extern "C" {
+
+int noa_dcs_mlp_create(noa_dcs_mlp **out, int process, int batch) {
+    g_merr[0] = '\0';
+    if (!out)
+        return mfail(NOA_DCS_ERROR_INVALID_VALUE, "NULL model pointer");
+    *out = nullptr;
+    if (process != NOA_DCS_PAIR_PRODUCTION && process != NOA_DCS_PHOTONUCLEAR)
+        return mfail(NOA_DCS_ERROR_NOT_SUPPORTED, "the surrogate covers pair production and photonuclear");
+    if (batch < 128 || batch > (1 << 20) || batch % 128)
+        return mfail(NOA_DCS_ERROR_INVALID_VALUE, "batch must be a multiple of 128 in [128, 2^20]");
+    cudaError_t e = set_gemm_smem();
+    if (e != cudaSuccess)
+        return mfail(NOA_DCS_ERROR_CUDA, "cudaFuncSetAttribute", e);
+    noa_dcs_mlp *m = new (std::nothrow) noa_dcs_mlp();
+    if (!m)
+        return mfail(NOA_DCS_ERROR_INVALID_VALUE, "out of host memory");
+    m->process = process;
+    m->batch = batch;
+    const size_t act = sizeof(float) * (size_t)batch * H;
+    float **acts[] = {&m->Z1, &m->H1, &m->Z2, &m->H2, &m->Z3, &m->H3, &m->D3, &m->D2, &m->D1};
+    e = cudaSuccess;
+    for (float **a : acts)
+        if (e == cudaSuccess)
+            e = cudaMalloc((void **)a, act);
+    if (e == cudaSuccess)
+        e = cudaMalloc((void **)&m->P, sizeof(float) * NPARAM * 4);
+    if (e == cudaSuccess)
+        e = cudaMalloc((void **)&m->Wb, sizeof(__nv_bfloat16) * 4 * H * H);
+    if (e == cudaSuccess)
+        e = cudaMalloc((void **)&m->Xb, sizeof(float) * (size_t)batch * (IN + 1) + sizeof(float));
+    if (e != cudaSuccess) {
+        for (float **a : acts)
+            cudaFree(*a);
+        cudaFree(m->P);
+        cudaFree(m->Wb);
+        cudaFree(m->Xb);
+        delete m;
+        return mfail(NOA_DCS_ERROR_CUDA, "model allocation", e);
+    }
+    m->G = m->P + NPARAM;
+    m->Mm = m->G + NPARAM;
+    m->V = m->Mm + NPARAM;
+    m->Tb = m->Xb + (size_t)batch * IN;
+    m->loss = m->Tb + batch;
+    cudaMemset(m->P, 0, sizeof(float) * NPARAM * 4);
+    cudaMemset(m->Wb, 0, sizeof(__nv_bfloat16) * 4 * H * H);
+    *out = m;
+    return NOA_DCS_SUCCESS;
+}
+
+int noa_dcs_mlp_set_params(noa_dcs_mlp *m, const float *params, const float *adam_m, const float *adam_v,
+                           int64_t step, const float *norm) {
+    if (!m || !params || !norm)
+        return mfail(NOA_DCS_ERROR_INVALID_VALUE, "NULL argument");
+    cudaError_t e = cudaMemcpy(m->P, params, sizeof(float) * NPARAM, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess)
+        e = adam_m ? cudaMemcpy(m->Mm, adam_m, sizeof(float) * NPARAM, cudaMemcpyHostToDevice)
+                   : cudaMemset(m->Mm, 0, sizeof(float) * NPARAM);
+    if (e == cudaSuccess)
+        e = adam_v ? cudaMemcpy(m->V, adam_v, sizeof(float) * NPARAM, cudaMemcpyHostToDevice)
+                   : cudaMemset(m->V, 0, sizeof(float) * NPARAM);
+    if (e != cudaSuccess)
+        return mfail(NOA_DCS_ERROR_CUDA, "cudaMemcpy(params)", e);
+    mlp_round_weights_kernel<<<64, 256>>>(m->P, m->Wb);
+    if ((e = cudaDeviceSynchronize()) != cudaSuccess)
+        return mfail(NOA_DCS_ERROR_CUDA, "round weights", e);
+    m->step = step;
+    std::memcpy(m->norm, norm, sizeof m->norm);
+    return NOA_DCS_SUCCESS;
+}
+
+int noa_dcs_mlp_get_params(noa_dcs_mlp *m, float *params, float *adam_m, float *adam_v, int64_t *step) {
+    if (!m || !params)
+        return mfail(NOA_DCS_ERROR_INVALID_VALUE, "NULL argument");
+    cudaError_t e = cudaMemcpy(params, m->P, sizeof(float) * NPARAM, cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess && adam_m)
+        e = cudaMemcpy(adam_m, m->Mm, sizeof(float) * NPARAM, cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess && adam_v)
+        e = cudaMemcpy(adam_v, m->V, sizeof(float) * NPARAM, cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess)
+        return mfail(NOA_DCS_ERROR_CUDA, "cudaMemcpy(params)", e);
+    if (step)
+        *step = m->step;
+    return NOA_DCS_SUCCESS;
+}
+
+int noa_dcs_mlp_prepare(int process, const double *K, const double *q, const uint8_t *elem, int64_t n,
+                        const noa_dcs_element *elements, int n_elements, double mass, float *Xraw, float *R,
+                        uint8_t *valid, void *stream) {
+    g_merr[0] = '\0';
+    if (process != NOA_DCS_PAIR_PRODUCTION && process != NOA_DCS_PHOTONUCLEAR)
+        return mfail(NOA_DCS_ERROR_NOT_SUPPORTED, "the surrogate covers pair production and photonuclear");
+    if (n < 0 || n_elements < 1 || n_elements > 16 || !elements)
+        return mfail(NOA_DCS_ERROR_INVALID_VALUE, "bad sizes");
+    if (n == 0)
+        return NOA_DCS_SUCCESS;
+    noa_dcs_consts hc[16];
+    float hlogA[16];
+    for (int i = 0; i < n_elements; i++) {
+        noa_dcs_fill_consts(&hc[i], elements[i].A, elements[i].I, elements[i].Z, mass);
+        hlogA[i] = (float)std::log(elements[i].A);
+    }
+    // The element table (up to 16 constant sets) is staged through a small
+    // device buffer that lives until this call's work is done (synchronised
+    // below); data preparation is off the evaluation path.
+    noa_dcs_consts *dc = nullptr;
+    float *dl = nullptr;
+    cudaError_t e = cudaMalloc((void **)&dc, sizeof hc + sizeof hlogA);
+    if (e != cudaSuccess)
+        return mfail(NOA_DCS_ERROR_CUDA, "cudaMalloc(element table)", e);
+    dl = reinterpret_cast<float *>(dc + 16);
+    cudaStream_t s = (cudaStream_t)stream;
+    e = cudaMemcpyAsync(dc, hc, sizeof hc, cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(dl, hlogA, sizeof hlogA, cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess) {
+        const int64_t blocks = (n + 255) / 256;
+        const int grid = (int)(blocks < 152 * 16 ? blocks : 152 * 16);
+        if (process == NOA_DCS_PAIR_PRODUCTION)
+            mlp_prepare_kernel<NOA_DCS_PAIR_PRODUCTION><<<grid, 256, 0, s>>>(K, q, elem, n, dc, dl, Xraw, R, valid);
+        else
+            mlp_prepare_kernel<NOA_DCS_PHOTONUCLEAR><<<grid, 256, 0, s>>>(K, q, elem, n, dc, dl, Xraw, R, valid);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess)
+        e = cudaStreamSynchronize(s);
+    cudaFree(dc);
+    if (e != cudaSuccess)
+        return mfail(NOA_DCS_ERROR_CUDA, "prepare", e);
+    return NOA_DCS_SUCCESS;
+}
+
+int noa_dcs_mlp_train(noa_dcs_mlp *m, const float *X, const float *T, int64_t n, const int32_t *perm,
+                      int64_t n_steps, float lr, float lr_final, float *losses, void *stream) {
+    g_merr[0] = '\0';
+    if (!m || !X || !T || !perm || n < m->batch || n_steps < 0)
+        return mfail(NOA_DCS_ERROR_INVALID_VALUE, "bad training arguments (n must be at least one batch)");
+    cudaStream_t s = (cudaStream_t)stream;
+    const int B = m->batch;
+    const int64_t batches = n / B;
+    cudaError_t e = cudaSuccess;
+    for (int64_t i = 0; i < n_steps && e == cudaSuccess; i++) {
+        const int64_t b = (m->step) % batches;
+        mlp_gather_kernel<<<(B + 255) / 256, 256, 0, s>>>(X, T, perm + b * B, m->Xb, m->Tb, B);
+        cudaMemsetAsync(m->loss, 0, sizeof(float), s);
+        if ((e = backward(m, B, s)) != cudaSuccess)
+            break;
+        // cosine decay from lr to lr_final over the n_steps of this call
+        const double frac = n_steps > 1 ? (double)i / (double)(n_steps - 1) : 0.;
+        const float lr_i = (float)(lr_final + 0.5 * (lr - lr_final) * (1. + std::cos(M_PI * frac)));
+        m->step++;
+        const float b1 = 0.9f, b2 = 0.999f;
+        const float c1 = 1.f / (1.f - std::pow(b1, (float)m->step));
+        const float c2 = 1.f / (1.f - std::pow(b2, (float)m->step));
+        mlp_adam_kernel<<<(NPARAM + 255) / 256, 256, 0, s>>>(m->P, m->G, m->Mm, m->V, m->Wb, lr_i, b1, b2, 1e-8f,
+                                                             c1, c2);
+        if (losses)
+            cudaMemcpyAsync(losses + i, m->loss, sizeof(float), cudaMemcpyDeviceToDevice, s);
+        e = cudaGetLastError();
+    }
+    if (e != cudaSuccess)
+        return mfail(NOA_DCS_ERROR_CUDA, "training step", e);
+    return NOA_DCS_SUCCESS;
+}
+
+int noa_dcs_mlp_predict(noa_dcs_mlp *m, const float *X, float *out, int64_t n, void *stream) {
+    g_merr[0] = '\0';
+    if (!m || (n > 0 && (!X || !out)) || n < 0)
+        return mfail(NOA_DCS_ERROR_INVALID_VALUE, "bad arguments");
+    cudaStream_t s = (cudaStream_t)stream;
+    for (int64_t off = 0; off < n; off += m->batch) {
+        const int M = (int)((n - off) < m->batch ? (n - off) : m->batch);
+        cudaMemcpyAsync(m->Xb, X + off * IN, sizeof(float) * IN * M, cudaMemcpyDeviceToDevice, s);
+        const cudaError_t e = forward(m, M, out + off, s);
+        if (e != cudaSuccess)
+            return mfail(NOA_DCS_ERROR_CUDA, "forward", e);
+    }
+    return NOA_DCS_SUCCESS;
+}
+
+int noa_dcs_mlp_gradient(noa_dcs_mlp *m, const float *X, const float *T, int n, float *grad, float *loss,
+                         void *stream) {
+    g_merr[0] = '\0';
+    if (!m || !X || !T || !grad || n < 1 || n > m->batch)
+        return mfail(NOA_DCS_ERROR_INVALID_VALUE, "bad arguments (1 <= n <= batch)");
+    cudaStream_t s = (cudaStream_t)stream;
+    cudaMemcpyAsync(m->Xb, X, sizeof(float) * IN * n, cudaMemcpyDeviceToDevice, s);
+    cudaMemcpyAsync(m->Tb, T, sizeof(float) * n, cudaMemcpyDeviceToDevice, s);
+    cudaMemsetAsync(m->loss, 0, sizeof(float), s);
+    cudaError_t e = backward(m, n, s);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(grad, m->G, sizeof(float) * NPARAM, cudaMemcpyDeviceToDevice, s);
+    if (e == cudaSuccess && loss)
+        e = cudaMemcpyAsync(loss, m->loss, sizeof(float), cudaMemcpyDeviceToDevice, s);
+    if (e != cudaSuccess)
+        return mfail(NOA_DCS_ERROR_CUDA, "gradient", e);
+    return NOA_DCS_SUCCESS;
+}
+
+int noa_dcs_mlp_destroy(noa_dcs_mlp *m) {
+    if (!m)
+        return NOA_DCS_SUCCESS;
+    float *acts[] = {m->Z1, m->H1, m->Z2, m->H2, m->Z3, m->H3, m->D3, m->D2, m->D1};
+    for (float *a : acts)
+        cudaFree(a);
+    cudaFree(m->P);
+    cudaFree(m->Wb);
+    cudaFree(m->Xb);
+    delete m;
+    return NOA_DCS_SUCCESS;
+}
+
+const char *noa_dcs_mlp_last_error(void) { return g_merr; }
+
+// Internal accessor for the inference translation unit (mlp_infer.cu).
+int noa_dcs_mlp_handles(noa_dcs_mlp *m, int *process, const float **P, const void **Wb, const float **norm) {
+    if (!m)
+        return 1;
+    *process = m->process;
+    *P = m->P;
+    *Wb = m->Wb;
+    *norm = m->norm;
+    return 0;
+}
+
+} // extern "C"

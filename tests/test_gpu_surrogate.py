@@ -1,0 +1,87 @@
+"""GPU tests of the surrogate's inference (noa_dcs_mlp_infer): the tcgen05
+network kernel against the validated tensor-core forward (mma.sync path),
+the trust grid and the FP32C fallback against the oracle, and what the
+trained network gains over the kernels without it."""
+import numpy as np
+import pytest
+import torch
+
+import oracle
+from noa_gb300.batched import batch_inputs
+from noa_gb300.elements import BATCH_Z, ELEMENTS, MUON_MASS
+from noa_gb300.surrogate import GRID, train_recipe
+from tests.parity import rel_stats
+
+pytestmark = pytest.mark.gpu
+
+COUNTS = [40000] * len(BATCH_Z)
+
+
+@pytest.fixture(scope="module", params=[1, 2], ids=["pair_production", "photonuclear"])
+def trained(request, cuda_device):
+    # a short version of the training recipe (the bench runs the full one)
+    return train_recipe(request.param, n_valid=2_000_000, steps1=15_000, steps2=30_000, batch=8192,
+                        heldout=1_000_000)
+
+
+def queries():
+    K, q = batch_inputs(BATCH_Z, COUNTS, seed=424242)
+    return torch.from_numpy(K).cuda(), torch.from_numpy(q).cuda(), K, q
+
+
+def oracle_all(process, K, q):
+    out, o = [], 0
+    for z, c in zip(BATCH_Z, COUNTS):
+        out.append(oracle.dcs(process, K[o:o + c], q[o:o + c], ELEMENTS[z], MUON_MASS))
+        o += c
+    return np.concatenate(out)
+
+
+def test_tcgen05_network_matches_reference_forward(trained):
+    """All cells trusted: every open pair goes through the tcgen05 kernel; its
+    result equals exp(baseline + residual) of the mma.sync forward."""
+    s = trained
+    tk, tq, K, q = queries()
+    ones = np.ones((len(BATCH_Z), *GRID), dtype=np.uint8)
+    out, st = s.infer(tk, tq, COUNTS, trust=ones)
+    assert st["status"] == 0
+    exp = oracle_all(s.process, K, q)
+    got = out.cpu().numpy()
+    assert np.array_equal(got == 0, exp == 0)
+    # reference: same features / baseline through the validated forward
+    e = np.repeat(np.arange(len(BATCH_Z)), COUNTS).astype(np.uint8)
+    Xraw, R, valid = s.prepare(K, q, e)
+    X = s.normalise(Xraw[valid])
+    pred = s.residual(s.predict(X)).double().cpu().numpy()
+    base = np.log(exp[valid.cpu().numpy()]) - R[valid].double().cpu().numpy()   # FP64 baseline
+    ref = np.exp(base + pred)
+    g = got[valid.cpu().numpy()]
+    rel = np.abs(g - ref) / ref
+    assert np.quantile(rel, 0.999) < 2e-4 and rel.max() < 1e-3, (np.quantile(rel, 0.999), rel.max())
+    assert st["network"] == int(valid.sum()) and st["fallback"] == 0
+
+
+def test_trusted_inference_within_bound(trained):
+    s = trained
+    tk, tq, K, q = queries()
+    out, st = s.infer(tk, tq, COUNTS)
+    exp = oracle_all(s.process, K, q)
+    got = out.cpu().numpy()
+    stats = rel_stats(got, exp)
+    assert stats["zero_agree"] and stats["nonfinite_agree"]
+    nz = exp != 0
+    rel = np.abs(got[nz] - exp[nz]) / exp[nz]
+    print(s.process, st, "frac>1e-3", float((rel > 1e-3).mean()), "max", float(rel.max()), s.info)
+    assert st["network"] > 0.1 * nz.sum()       # the network answers a real share
+    assert float((rel > 1e-3).mean()) < 2e-3     # held-out-trusted cells generalise
+    assert float(np.median(rel)) < 1e-4
+
+
+def test_untrusted_everywhere_is_the_fp32c_kernel(trained):
+    s = trained
+    tk, tq, K, q = queries()
+    zeros = np.zeros((len(BATCH_Z), *GRID), dtype=np.uint8)
+    out, st = s.infer(tk, tq, COUNTS, trust=zeros)
+    assert st["network"] == 0
+    stats = rel_stats(out.cpu().numpy(), oracle_all(s.process, K, q))
+    assert stats["zero_agree"] and stats["max"] <= 1e-6
