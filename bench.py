@@ -56,6 +56,8 @@ def parse_args():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-batched", action="store_true")
     ap.add_argument("--no-integrals", action="store_true")
+    ap.add_argument("--no-surrogate", action="store_true")
+    ap.add_argument("--surrogate-queries", type=int, default=100_000_000)
     return ap.parse_args()
 
 
@@ -331,6 +333,75 @@ def time_integrals(torch, args, with_cpu):
     return res
 
 
+def time_surrogate(torch, args):
+    """Learned surrogate (pair production, photonuclear): trained here on the
+    GPU (plain-kernel data, tensor-core forward / backward, Adam; moderate
+    recipe), then evaluated on `surrogate_queries` seeded pairs over the 10
+    elements: the network answers the pairs of trusted cells (held-out error
+    <= 5e-4), the FP32C kernel the rest.  Compared with the plain FP64 kernel
+    and the FP32C kernel (batched engine, one launch) on the same pairs; error
+    against the plain FP64 output."""
+    from noa_gb300.batched import BatchPlan, batch_inputs
+    from noa_gb300.elements import BATCH_Z, ELEMENTS, MUON_MASS
+    from noa_gb300.surrogate import train_recipe
+    nq = args.surrogate_queries
+    counts = [nq // len(BATCH_Z)] * len(BATCH_Z)
+    counts[-1] += nq - sum(counts)
+    K, q = batch_inputs(BATCH_Z, counts, seed=777)
+    tk, tq = torch.from_numpy(K).cuda(), torch.from_numpy(q).cuda()
+    del K, q
+    stream = torch.cuda.current_stream()
+    steps = max(1, min(args.steps, 3))
+    res = {"queries": nq, "elements_Z": list(BATCH_Z), "error_bound": 1e-3}
+
+    def timed(fn):
+        fn()
+        torch.cuda.synchronize()
+        s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        s.record(stream)
+        for _ in range(steps):
+            fn()
+        e.record(stream)
+        torch.cuda.synchronize()
+        return s.elapsed_time(e) * 1e-3 / steps
+
+    for p, name in ((1, "pair_production"), (2, "photonuclear")):
+        sur = train_recipe(p, n_valid=6_000_000, steps1=30_000, steps2=90_000, batch=8192, heldout=2_000_000)
+        ref = torch.empty_like(tk)
+        out = torch.empty_like(tk)
+        entry = {"training": sur.info}
+        with BatchPlan(p, [ELEMENTS[z] for z in BATCH_Z], counts, MUON_MASS, "fp64") as plan:
+            plan.set_tile(256, 8, 2)
+            entry["fp64_s"] = timed(lambda: plan.execute_graph(ref, tk, tq))
+        with BatchPlan(p, [ELEMENTS[z] for z in BATCH_Z], counts, MUON_MASS, "fp32c") as plan:
+            plan.set_tile(256, 8, 2)
+            entry["fp32c_s"] = timed(lambda: plan.execute_graph(out, tk, tq))
+        stats = {}
+
+        def run():
+            o, st = sur.infer(tk, tq, counts)
+            stats.update(st)
+            out.copy_(o)
+        entry["surrogate_s"] = timed(run)
+        nz = ref != 0
+        rel = ((out[nz] - ref[nz]).abs() / ref[nz]).float()
+        entry.update({
+            "evals_per_s": {"fp64": nq / entry["fp64_s"], "fp32c": nq / entry["fp32c_s"],
+                            "surrogate": nq / entry["surrogate_s"]},
+            "speedup_vs_fp64": entry["fp64_s"] / entry["surrogate_s"],
+            "speedup_vs_fp32c": entry["fp32c_s"] / entry["surrogate_s"],
+            "network_share_of_open": stats["network"] / max(1, int(nz.sum())),
+            "status": stats["status"],
+            "max_rel": float(rel.max()), "median_rel": float(rel.median()),
+            "frac_above_1e-3": float((rel > 1e-3).float().mean()),
+            "zero_pattern_equal": bool(torch.equal(out == 0, ref == 0)),
+        })
+        res[name] = entry
+        sur.close()
+        del ref, out
+    return res
+
+
 def load_traffic():
     path = os.path.join(ROOT, "profiles", "traffic.json")
     try:
@@ -467,6 +538,8 @@ def run_ours(args):
         line["batched"] = time_batched(torch, args)
     if not args.no_integrals:
         line["recoil_integrals"] = time_integrals(torch, args, with_cpu=not args.no_cpu_baseline and world == 1)
+    if not args.no_surrogate:
+        line["surrogate"] = time_surrogate(torch, args)
     if not args.no_cpu_baseline and world == 1:
         cb = cpu_reference_rate(min(n, 1_000_000))
         line["cpu_baseline"] = {"value": cb["value"], "unit": "evals/s", "cores": cb["cores"], "kind": "port",

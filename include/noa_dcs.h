@@ -185,7 +185,8 @@ int noa_dcs_mlp_set_params(noa_dcs_mlp *model, const float *params, const float 
 int noa_dcs_mlp_get_params(noa_dcs_mlp *model, float *params, float *adam_m, float *adam_v, int64_t *step);
 /* Training data from the FP64 kernels: for pairs (K[i], q[i]) of element
  * elements[elem[i]], raw features Xraw[i][4], residual R[i] = log DCS - baseline
- * and valid[i] (0 where the DCS is zero).  Device buffers; synchronous. */
+ * and state[i]: 1 open with DCS > 0, 0 closed by the kinematic bounds, 2 open
+ * by the bounds but DCS = 0.  Device buffers; synchronous. */
 int noa_dcs_mlp_prepare(int process, const double *K, const double *q, const uint8_t *elem, int64_t n,
                         const noa_dcs_element *elements, int n_elements, double mass, float *Xraw, float *R,
                         uint8_t *valid, void *stream);

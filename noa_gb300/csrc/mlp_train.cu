@@ -304,8 +304,10 @@ __global__ void mlp_gather_kernel(const float *X, const float *T, const int32_t 
 }
 
 // Training data: raw features and the residual target from the FP64 plain
-// kernels (dcs_fp64.cuh).  valid = 0 for closed pairs (DCS = 0) and pairs
-// whose DCS underflows the baseline's log.
+// kernels (dcs_fp64.cuh).  state: 1 = open pair with DCS > 0 (a training
+// sample), 0 = closed by the kinematic bounds, 2 = open by the bounds but with
+// DCS = 0 (every screening term clamped) or no finite baseline -- cells that
+// hold such pairs must not be answered by the network.
 template <int PROC>
 __global__ void mlp_prepare_kernel(const double *K, const double *q, const uint8_t *elem, int64_t n,
                                    const noa_dcs_consts *consts, const float *logA, float *Xraw, float *R,
@@ -313,7 +315,8 @@ __global__ void mlp_prepare_kernel(const double *K, const double *q, const uint8
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
         const noa_dcs_consts &c = consts[elem[i]];
         double base;
-        bool ok = baseline<PROC>(K[i], q[i], c, base);
+        const bool open = baseline<PROC>(K[i], q[i], c, base);
+        bool ok = open;
         double d = 0.;
         if (ok) {
             d = PROC == NOA_DCS_PAIR_PRODUCTION ? noa_dcs::pprod_fp64(K[i], q[i], c) : noa_dcs::photo_fp64(K[i], q[i], c);
@@ -325,7 +328,7 @@ __global__ void mlp_prepare_kernel(const double *K, const double *q, const uint8
         Xraw[i * IN + 2] = (float)c.Zd * 0.01f;
         Xraw[i * IN + 3] = logA[elem[i]];
         R[i] = ok ? (float)(log(d) - base) : 0.f;
-        valid[i] = ok ? 1 : 0;
+        valid[i] = ok ? 1 : (open ? 2 : 0);
     }
 }
 

@@ -132,7 +132,10 @@ class Surrogate:
 
     # ------------------------------------------------------------ data
     def prepare(self, K, q, elem):
-        """Raw features, residual targets and validity from the FP64 kernels."""
+        """Raw features, residual targets and validity from the FP64 kernels.
+        Returns (Xraw, R, valid, open_zero): valid marks training samples
+        (open, DCS > 0); open_zero marks pairs open by the kinematic bounds
+        whose DCS is nevertheless 0."""
         dev = torch.device("cuda")
         tK = torch.as_tensor(K, dtype=torch.float64, device=dev)
         tq = torch.as_tensor(q, dtype=torch.float64, device=dev)
@@ -144,7 +147,7 @@ class Surrogate:
         els = (_lib.Element * len(self.elements_z))(*[_lib.element_struct(ELEMENTS[z]) for z in self.elements_z])
         _check(self.lib.noa_dcs_mlp_prepare(self.process, _ptr(tK), _ptr(tq), _ptr(te), n, els,
                                             len(self.elements_z), self.mass, _ptr(X), _ptr(R), _ptr(V), _stream()))
-        return X, R, V.bool()
+        return X, R, V == 1, V == 2
 
     def fit_norm(self, Xraw, R):
         lo = Xraw.min(0).values.cpu().numpy()
@@ -213,11 +216,12 @@ class Surrogate:
         c = (elem.long() * GRID[0] + ik.clamp(0, GRID[0] - 1)) * GRID[1] + inu.clamp(0, GRID[1] - 1)
         return torch.where(inside, c, torch.full_like(c, -1))
 
-    def build_trust(self, Xraw, R, valid, elem, bound=1e-3, safety=0.5, min_count=8):
+    def build_trust(self, Xraw, R, valid, elem, bound=1e-3, safety=0.5, min_count=8, open_zero=None):
         """Trust grid from a held-out set: a cell is trusted when all its
         held-out samples have |predicted - true| log DCS below safety * bound
-        (|d log DCS| is the relative DCS error to first order) and it holds at
-        least min_count of them."""
+        (|d log DCS| is the relative DCS error to first order), it holds at
+        least min_count of them, and none of its held-out pairs is open by the
+        kinematic bounds with DCS = 0 (the network cannot return 0)."""
         Xv, Rv, ev = Xraw[valid], R[valid], elem[valid]
         X, _ = self.normalise(Xv, Rv)
         err = (self.residual(self.predict(X)) - Rv).abs()
@@ -229,6 +233,10 @@ class Surrogate:
         worst.scatter_reduce_(0, cell[keep], err[keep], reduce="amax")
         count.scatter_add_(0, cell[keep], torch.ones_like(cell[keep]))
         trust = (worst <= safety * bound) & (count >= min_count)
+        if open_zero is not None and bool(open_zero.any()):
+            zc = self.cells(Xraw[open_zero], elem[open_zero])
+            zc = zc[zc >= 0]
+            trust[zc] = False
         self.trust = trust.to(torch.uint8).cpu().numpy().reshape(len(self.elements_z), *GRID)
         return {"cells_trusted": int(trust.sum()), "cells_with_data": int((count > 0).sum()),
                 "heldout_err_max": float(err.max()), "heldout_err_median": float(err.median()),
@@ -279,7 +287,7 @@ def train_recipe(process, n_valid=10_000_000, steps1=60_000, steps2=150_000, bat
     t0 = time.time()
     K, q, e = training_pairs(process, n_valid)
     s = Surrogate(process, batch=batch)
-    Xraw, R, valid = s.prepare(K, q, e)
+    Xraw, R, valid, _ = s.prepare(K, q, e)
     et = torch.as_tensor(e, device="cuda")
     Xv, Rv, ev = Xraw[valid], R[valid], et[valid]
     s.fit_norm(Xv, Rv)
@@ -287,7 +295,7 @@ def train_recipe(process, n_valid=10_000_000, steps1=60_000, steps2=150_000, bat
     X, T = s.normalise(Xv, Rv)
     s.fit(X, T, steps=steps1, lr=2e-3, lr_final=2e-5, seed=seed)
     Kh, qh, eh = training_pairs(process, heldout, seed=12345)
-    Xh, Rh, vh = s.prepare(Kh, qh, eh)
+    Xh, Rh, vh, zh = s.prepare(Kh, qh, eh)
     eht = torch.as_tensor(eh, device="cuda")
     Xn, _ = s.normalise(Xh[vh], Rh[vh])
     err = (s.residual(s.predict(Xn)) - Rh[vh]).abs()
@@ -298,7 +306,7 @@ def train_recipe(process, n_valid=10_000_000, steps1=60_000, steps2=150_000, bat
     tc = s.cells(Xv, ev)
     keep = (tc >= 0) & (worst[tc.clamp(min=0)] <= keep_err)
     s.fit(X[keep].contiguous(), T[keep].contiguous(), steps=steps2, lr=5e-4, lr_final=5e-6, seed=seed + 1)
-    info = s.build_trust(Xh, Rh, vh, eht, bound=bound)
+    info = s.build_trust(Xh, Rh, vh, eht, bound=bound, open_zero=zh)
     info.update({"train_seconds": time.time() - t0, "training_pairs": int(Xv.shape[0]),
                  "stage2_pairs": int(keep.sum()), "steps": steps1 + steps2, "batch": batch})
     if log:

@@ -94,7 +94,7 @@ def test_prediction_matches_cpu_forward(cuda_device):
 def test_training_data_from_the_plain_kernel(cuda_device, process):
     K, q, e = training_pairs(process, 20000)
     s = Surrogate(process)
-    Xraw, R, valid = s.prepare(K, q, e)
+    Xraw, R, valid, _ = s.prepare(K, q, e)
     Xraw, R, valid = Xraw.cpu().numpy(), R.cpu().numpy(), valid.cpu().numpy()
     for i, z in enumerate(BATCH_Z):
         m = e == i
@@ -108,7 +108,7 @@ def test_training_data_from_the_plain_kernel(cuda_device, process):
 def test_short_training_reduces_loss_and_checkpoint_roundtrip(cuda_device, tmp_path):
     K, q, e = training_pairs(1, 200_000)
     s = Surrogate(1, batch=2048)
-    Xraw, R, valid = s.prepare(K, q, e)
+    Xraw, R, valid, _ = s.prepare(K, q, e)
     Xraw, R = Xraw[valid], R[valid]
     s.fit_norm(Xraw, R)
     s.set_params(init_params(0), s.norm)
