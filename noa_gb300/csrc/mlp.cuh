@@ -50,9 +50,22 @@ struct Norm {
     float out_scale;  // r = out_shift + y / out_scale
 };
 
-__host__ __device__ __forceinline__ float silu(float z) { return z / (1.f + expf(-z)); }
+// SiLU and its derivative.  On the GPU through the MUFU exponential and an
+// approximate division (relative error ~2^-21), in training and inference
+// alike; z / (1 + inf) gives the correct limit 0.
+__host__ __device__ __forceinline__ float silu(float z) {
+#if defined(__CUDA_ARCH__)
+    return __fdividef(z, 1.f + __expf(-z));
+#else
+    return z / (1.f + expf(-z));
+#endif
+}
 __host__ __device__ __forceinline__ float dsilu(float z) {
+#if defined(__CUDA_ARCH__)
+    const float s = __fdividef(1.f, 1.f + __expf(-z));
+#else
     const float s = 1.f / (1.f + expf(-z));
+#endif
     return s * (1.f + z * (1.f - s));
 }
 
@@ -102,8 +115,10 @@ __device__ __forceinline__ bool baseline_fast(double K, double q, const noa_dcs_
         const float gamma = 1.f + (float)K * im;
         const float x1 = 6.f / (gamma * (1.f + (float)(K - q) * im));
         const float a = (x0 + 2.f * (1.f - x0) * x1) / (1.f + (1.f - x1) * sqrtf(fmaxf(1.f - x0, 0.f)));
+        // near argmin -> 1, -log(argmin) needs argmin's FP64 value
+        const float tmin = (a > 0.99f || !(x0 < 0.9f)) ? (float)d_log(pprod_argmin_exact(K, q, c)) : logf(a);
         base = logf((float)(c.pp_cZ * c.Zd * c.scale_A)) + logf(Emq) - logf(qf) - logf(Ef) +
-               logf((float)(mass + K)) + logf(-logf(a));
+               logf((float)(mass + K)) + logf(-tmin);
         return true;
     } else {
         if ((q < 1.) || (q < 2E-03 * K))

@@ -8,7 +8,7 @@
  *     Pairs inside the trained domain whose cell passed the held-out error
  *     check go to the network list; the others to the fallback list (both in
  *     the model's scratch, appended with warp-aggregated atomics).
- *  2. network (tcgen05): a persistent CTA of two warpgroups evaluates tiles of
+ *  2. network (tcgen05): a persistent CTA of four warpgroups evaluates tiles of
  *     128 listed pairs.  Row r of a tile is TMEM lane r.  Layer 1 (4 -> 128)
  *     and the output layer run in FP32 on the CUDA cores; the two 128 x 128
  *     layers run on the 5th-generation tensor cores: the activations are
@@ -18,8 +18,8 @@
  *     tcgen05.mma.cta_group::1.kind::f16 (M = N = 128, K = 16) for the three
  *     products A_hi W_hi + A_lo W_hi + A_hi W_lo, accumulating in FP32 in TMEM.
  *     tcgen05.commit signals an mbarrier; the epilogue reads the accumulator
- *     with tcgen05.ld (warpgroup 0 columns 0-63, warpgroup 1 columns 64-127
- *     of the same lanes), adds the bias and applies SiLU.
+ *     with tcgen05.ld (warpgroup g reads columns 32g .. 32g+31 of the same
+ *     128 lanes), adds the bias and applies SiLU.
  *     DCS = exp(baseline + residual), in float (1e-6 relative).
  *  3. fallback: the FP32C evaluation (dcs_fp32c.cuh) of the fallback list,
  *     with FP64 (dcs_fp64.cuh) for pairs above its tolerance.
@@ -42,7 +42,7 @@ using namespace noa_mlp;
 
 namespace {
 
-constexpr int NT = 256;                   // threads of the network kernel: 2 warpgroups
+constexpr int NT = 512;                   // threads of the network kernel: 4 warpgroups
 constexpr int TILE = 128;                 // rows (pairs) per tile = TMEM lanes
 constexpr int MAT = H * H * 2;            // bytes of one 128 x 128 BF16 operand
 constexpr int SMEM_NET = 6 * MAT + 1024;  // W2 hi/lo, W3 hi/lo, A hi/lo, alignment slack
@@ -135,20 +135,64 @@ __global__ void __launch_bounds__(256) classify_kernel(const __grid_constant__ I
     }
 }
 
+// FP32C evaluation of the fallback list; pairs above the tolerance go to a
+// shared-memory redo queue that full warps drain in FP64, so the FP64 work is
+// proportional to the redo fraction (as in dcs_fp32c.cu).
 template <int PROC>
 __global__ void __launch_bounds__(256) fallback_kernel(const __grid_constant__ InferParams p) {
+    __shared__ int32_t rq[512];
+    __shared__ uint8_t rs[512];
+    __shared__ int rn;
+    if (threadIdx.x == 0)
+        rn = 0;
+    __syncthreads();
     const unsigned long long cnt = p.counters[1];
-    for (unsigned long long e = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x; e < cnt;
-         e += (unsigned long long)gridDim.x * blockDim.x) {
-        const int32_t i = p.fb_idx[e];
-        const noa_dcs_consts &c = p.consts[p.fb_seg[e]];
-        const double K = p.K[i], q = p.q[i];
-        float est;
-        double v = PROC == NOA_DCS_PAIR_PRODUCTION ? noa_dcs::pprod_fp32c<true>(K, q, c, est)
-                                                   : noa_dcs::photo_fp32c<true>(K, q, c, est);
-        if (!(est <= p.tol))
-            v = PROC == NOA_DCS_PAIR_PRODUCTION ? noa_dcs::pprod_fp64(K, q, c) : noa_dcs::photo_fp64(K, q, c);
-        p.out[i] = v;
+    for (unsigned long long base = (unsigned long long)blockIdx.x * blockDim.x; base < cnt;
+         base += (unsigned long long)gridDim.x * blockDim.x) {
+        const unsigned long long e = base + threadIdx.x;
+        bool redo = false;
+        int32_t i = 0;
+        uint8_t sg = 0;
+        if (e < cnt) {
+            i = p.fb_idx[e];
+            sg = p.fb_seg[e];
+            const noa_dcs_consts &c = p.consts[sg];
+            float est;
+            const double v = PROC == NOA_DCS_PAIR_PRODUCTION ? noa_dcs::pprod_fp32c<true>(p.K[i], p.q[i], c, est)
+                                                             : noa_dcs::photo_fp32c<true>(p.K[i], p.q[i], c, est);
+            redo = !(est <= p.tol);
+            if (!redo)
+                p.out[i] = v;
+        }
+        const unsigned m = __ballot_sync(0xffffffffu, redo);
+        if (m) {
+            const int lane = threadIdx.x & 31;
+            int at = 0;
+            if (lane == 0)
+                at = atomicAdd(&rn, __popc(m));
+            at = __shfl_sync(0xffffffffu, at, 0);
+            if (redo) {
+                const int pos = at + __popc(m & ((1u << lane) - 1u));
+                rq[pos] = i;
+                rs[pos] = sg;
+            }
+        }
+        __syncthreads();
+        const bool last = base + (unsigned long long)gridDim.x * blockDim.x >= cnt;
+        while (rn >= (last ? 1 : 256)) {
+            const int n = rn, take = n < 256 ? n : 256;
+            if ((int)threadIdx.x < take) {
+                const int k = n - take + threadIdx.x;
+                const int32_t j = rq[k];
+                const noa_dcs_consts &c = p.consts[rs[k]];
+                p.out[j] = PROC == NOA_DCS_PAIR_PRODUCTION ? noa_dcs::pprod_fp64(p.K[j], p.q[j], c)
+                                                           : noa_dcs::photo_fp64(p.K[j], p.q[j], c);
+            }
+            __syncthreads();
+            if (threadIdx.x == 0)
+                rn = n - take;
+            __syncthreads();
+        }
     }
 }
 
@@ -261,23 +305,24 @@ __global__ void __launch_bounds__(NT, 1) network_kernel(const __grid_constant__ 
     unsigned char *W2h = sm, *W2l = sm + MAT, *W3h = sm + 2 * MAT, *W3l = sm + 3 * MAT;
     unsigned char *Ahi = sm + 4 * MAT, *Alo = sm + 5 * MAT;
     __shared__ float sW1[H * IN], sb1[H], sb2[H], sb3[H], sWo[H];
-    __shared__ float spart[TILE];
+    __shared__ float spart[3][TILE];
     __shared__ uint32_t tmem_slot;
     __shared__ __align__(8) unsigned long long mbar;
     __shared__ int s_abort;
 
     const int tid = threadIdx.x, warp = tid >> 5;
-    const int row = tid & 127, half = tid >> 7;  // row = TMEM lane, half = column half
+    const int row = tid & 127, quarter = tid >> 7;  // row = TMEM lane, quarter = column block of 32
     const unsigned long long cnt = p.counters[0];
 
-    // weights to shared memory (canonical layout) and registers / smem
-    for (int e = tid; e < H * H; e += NT) {
-        const int r = e / H, k = e % H;
+    // weights to shared memory (canonical layout): 8 consecutive k of a row are 16 contiguous bytes
+    for (int e = tid; e < H * H / 8; e += NT) {
+        const int r = e / (H / 8), k = (e % (H / 8)) * 8;
         const uint32_t o = canon_off(r, k);
-        *reinterpret_cast<__nv_bfloat16 *>(W2h + o) = Wb[e];
-        *reinterpret_cast<__nv_bfloat16 *>(W3h + o) = Wb[H * H + e];
-        *reinterpret_cast<__nv_bfloat16 *>(W2l + o) = Wb[2 * H * H + e];
-        *reinterpret_cast<__nv_bfloat16 *>(W3l + o) = Wb[3 * H * H + e];
+        const uint4 *src = reinterpret_cast<const uint4 *>(Wb) + e;
+        *reinterpret_cast<uint4 *>(W2h + o) = src[0];
+        *reinterpret_cast<uint4 *>(W3h + o) = src[H * H / 8];
+        *reinterpret_cast<uint4 *>(W2l + o) = src[2 * H * H / 8];
+        *reinterpret_cast<uint4 *>(W3l + o) = src[3 * H * H / 8];
     }
     for (int e = tid; e < H * IN; e += NT)
         sW1[e] = P[OFF_W1 + e];
@@ -312,8 +357,8 @@ __global__ void __launch_bounds__(NT, 1) network_kernel(const __grid_constant__ 
         const long long e = t * TILE + row;
         const bool valid = e < (long long)cnt;
         float4 f = valid ? p.net_feat[e] : make_float4(0.f, 0.f, 0.f, 0.f);
-        // layer 1 (FP32): this thread's 64 hidden units of its row
-        for (int k0 = half * 64; k0 < half * 64 + 64; k0 += 8) {
+        // layer 1 (FP32): this thread's 32 hidden units of its row
+        for (int k0 = quarter * 32; k0 < quarter * 32 + 32; k0 += 8) {
             float h[8];
 #pragma unroll
             for (int j = 0; j < 8; j++) {
@@ -346,8 +391,8 @@ __global__ void __launch_bounds__(NT, 1) network_kernel(const __grid_constant__ 
             if (s_abort)
                 break;
             const float *bias = layer ? sb3 : sb2;
-#pragma unroll 1
-            for (int c0 = half * 64; c0 < half * 64 + 64; c0 += 32) {
+            {
+                const int c0 = quarter * 32;
                 float v[32];
                 tmem_ld32(tmem + lane_base + layer * 128 + c0, v);
                 if (layer == 0) {
@@ -368,13 +413,13 @@ __global__ void __launch_bounds__(NT, 1) network_kernel(const __grid_constant__ 
         }
         if (s_abort)
             break;
-        // output: sum the two halves, DCS = exp(baseline + residual)
-        if (half == 1)
-            spart[row] = y;
+        // output: sum the four column blocks, DCS = exp(baseline + residual)
+        if (quarter > 0)
+            spart[quarter - 1][row] = y;
         fence_before();
         __syncthreads();
-        if (half == 0 && valid) {
-            const float yy = y + spart[row] + bo;
+        if (quarter == 0 && valid) {
+            const float yy = y + spart[0][row] + spart[1][row] + spart[2][row] + bo;
             const float r = p.norm.out_shift + yy / p.norm.out_scale;
             p.out[p.net_idx[e]] = (double)expf(p.net_base[e] + r);
         }

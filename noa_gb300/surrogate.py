@@ -313,3 +313,50 @@ def train_recipe(process, n_valid=10_000_000, steps1=60_000, steps2=150_000, bat
         log(info)
     s.info = info
     return s
+
+
+def _main(argv=None):
+    """Command line: train and save a surrogate, or evaluate a saved one.
+
+        python -m noa_gb300.surrogate train PROCESS OUT.npz [--pairs N] [--steps1 S] [--steps2 S]
+        python -m noa_gb300.surrogate infer MODEL.npz [--queries N] [--repeat R]
+    """
+    import argparse
+    import json
+    import time
+
+    from .batched import batch_inputs
+    ap = argparse.ArgumentParser(prog="python -m noa_gb300.surrogate")
+    sub = ap.add_subparsers(dest="cmd", required=True)
+    t = sub.add_parser("train")
+    t.add_argument("process", type=int, choices=[1, 2])
+    t.add_argument("out")
+    t.add_argument("--pairs", type=float, default=1e7)
+    t.add_argument("--steps1", type=int, default=60_000)
+    t.add_argument("--steps2", type=int, default=150_000)
+    i = sub.add_parser("infer")
+    i.add_argument("model")
+    i.add_argument("--queries", type=float, default=1e7)
+    i.add_argument("--repeat", type=int, default=3)
+    a = ap.parse_args(argv)
+    if a.cmd == "train":
+        s = train_recipe(a.process, n_valid=int(a.pairs), steps1=a.steps1, steps2=a.steps2)
+        s.save(a.out)
+        print(json.dumps(s.info))
+        return
+    s = Surrogate.load(a.model)
+    nq = int(a.queries)
+    counts = [nq // len(s.elements_z)] * len(s.elements_z)
+    counts[-1] += nq - sum(counts)
+    K, q = batch_inputs(s.elements_z, counts, seed=777)
+    tk, tq = torch.from_numpy(K).cuda(), torch.from_numpy(q).cuda()
+    st = {}
+    for _ in range(a.repeat):
+        t0 = time.perf_counter()
+        out, st = s.infer(tk, tq, counts)
+        dt = time.perf_counter() - t0
+    print(json.dumps({"queries": nq, "seconds": dt, "evals_per_s": nq / dt, **st}))
+
+
+if __name__ == "__main__":
+    _main()
