@@ -66,6 +66,23 @@ def dist_env():
             int(os.environ.get("LOCAL_RANK", 0)))
 
 
+def shard_offset(rank, n):
+    """First workload element of a rank's shard: every rank evaluates its own
+    n pairs of the seeded stream (weak scaling, no data exchange)."""
+    return rank * n
+
+
+def reduce_max(value, world, device=None):
+    """Max of a float over ranks (the slowest rank's time); identity for one rank."""
+    if world <= 1:
+        return value
+    import torch
+    import torch.distributed as tdist
+    t = torch.tensor([value], dtype=torch.float64, device=device)
+    tdist.all_reduce(t, op=tdist.ReduceOp.MAX)
+    return float(t.item())
+
+
 # ---------------------------------------------------------------- CPU side
 def cpu_reference_rate(n_sample, reps=3, offset=0):
     """Evaluations/s of the oracle (reference algorithm) with every host
@@ -424,7 +441,7 @@ def run_ours(args):
         tdist.init_process_group("nccl", device_id=torch.device("cuda", local))
     lib = _lib.load()
     n = args.n
-    K, q = kinetic_recoil(n, offset=rank * n)  # each rank its own shard: weak scaling
+    K, q = kinetic_recoil(n, offset=shard_offset(rank, n))  # each rank its own shard: weak scaling
     dev = torch.device("cuda", local)
     tk = torch.from_numpy(K).to(dev)
     tq = torch.from_numpy(q).to(dev)
@@ -463,10 +480,7 @@ def run_ours(args):
     elapsed = start.elapsed_time(end) * 1e-3
     per_proc_s = {name: sum(evs[s][p][0].elapsed_time(evs[s][p][1]) for s in range(args.steps)) * 1e-3
                   for p, name in enumerate(PROCESSES)}
-    if world > 1:
-        t = torch.tensor([elapsed], device=dev, dtype=torch.float64)
-        tdist.all_reduce(t, op=tdist.ReduceOp.MAX)
-        elapsed = float(t.item())
+    elapsed = reduce_max(elapsed, world, dev)
     value = world * 4 * n * args.steps / elapsed
 
     # e2e: host buffers in pinned memory, through noa_dcs_vmap_host, copies timed.
@@ -488,10 +502,7 @@ def run_ours(args):
         for _ in range(e2e_steps):
             host_step()
         t_e2e = time.perf_counter() - t0
-        if world > 1:
-            t = torch.tensor([t_e2e], device=dev, dtype=torch.float64)
-            tdist.all_reduce(t, op=tdist.ReduceOp.MAX)
-            t_e2e = float(t.item())
+        t_e2e = reduce_max(t_e2e, world, dev)
         e2e = {"value": world * 4 * n * e2e_steps / t_e2e, "unit": "evals/s",
                "h2d_bytes_per_step": 4 * 2 * 8 * n, "d2h_bytes_per_step": 4 * 8 * n, "steps": e2e_steps,
                "path": "noa_dcs_vmap_host (pinned host buffers, chunked copy/compute pipeline)"}

@@ -100,9 +100,22 @@ __device__ __forceinline__ bool baseline(double K, double q, const noa_dcs_const
 // exact IEEE decision near a bound (the FP64 kernels' float-first checks), and
 // the baseline as a sum of float logs (about 1e-6 absolute, far below the
 // surrogate's 1e-3).  Returns false for a closed pair.
+// Float pre-check of the reference's first early returns: true only where
+// the pair is certainly closed (margins of 1e-5 relative, far above float
+// rounding); the exact checks decide everything else.
+template <int PROC>
+__device__ __forceinline__ bool surely_closed(double K, double q, const noa_dcs_consts &c) {
+    const float Kf = (float)K, qf = (float)q;
+    if (PROC == NOA_DCS_PAIR_PRODUCTION)
+        return qf < (float)(4. * noa_dcs::ME) * 0.99999f || qf > (Kf + (float)c.pp_kmax_shift) * 1.00001f;
+    return qf < 0.99999f || qf < 2E-03f * Kf * 0.99999f;
+}
+
 template <int PROC>
 __device__ __forceinline__ bool baseline_fast(double K, double q, const noa_dcs_consts &c, float &base) {
     using namespace noa_dcs;
+    if (surely_closed<PROC>(K, q, c))
+        return false;
     const double mass = c.mass;
     const double E = K + mass;
     const float Ef = (float)E, qf = (float)q, Emq = (float)(E - q);
