@@ -350,6 +350,66 @@ def time_integrals(torch, args, with_cpu):
     return res
 
 
+def time_transport(torch, args, with_cpu):
+    """Per-K transport functions over 1e5 seeded kinetic energies, FP64:
+    soft_scattering (dcs.hh:941-952: 102 photonuclear DCS nodes per K) and the
+    elastic chain coulomb_data -> coulomb_transport(mu = 1) -> hard_scattering
+    (dcs.hh:499-872) for standard rock; the CPU oracle is timed on the first
+    5000 energies (soft scattering, every host thread) or all of them
+    (elastic chain, one thread: the reference's loops are serial)."""
+    import oracle
+    from noa_gb300 import dcs
+    from noa_gb300.elements import MUON_MASS, STANDARD_ROCK
+    from noa_gb300.workload import kinetic_recoil
+    nk = 100_000
+    K, _ = kinetic_recoil(nk, offset=1 << 31)
+    tk = torch.from_numpy(K).cuda()
+    out = torch.empty_like(tk)
+    f64 = dict(dtype=torch.float64, device="cuda")
+    fCM, screen, fspin, il = (torch.empty(nk, 2, **f64), torch.empty(nk, 9, **f64), torch.empty(nk, **f64),
+                              torch.empty(nk, **f64))
+    G, mu0, lb_h = torch.empty(nk, 2, **f64), torch.empty(nk, **f64), torch.empty(nk, **f64)
+    one = torch.tensor(1.0, **f64)
+
+    def soft():
+        dcs.soft_scattering(out, tk)
+
+    def chain():
+        dcs.coulomb_data(fCM, screen, fspin, il, tk)
+        dcs.coulomb_transport(G, screen, fspin, one)
+        dcs.hard_scattering(mu0, lb_h, G.view(1, nk, 2), fCM.view(1, nk, 2), screen.view(1, nk, 9),
+                            il.view(1, nk), fspin.view(1, nk))
+
+    stream = torch.cuda.current_stream()
+    res = {"n_kinetic": nk}
+    for name, fn in (("soft_scattering", soft), ("coulomb_chain", chain)):
+        for _ in range(max(1, args.warmup)):
+            fn()
+        s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        steps = max(1, min(args.steps, 5))
+        torch.cuda.synchronize()
+        s.record(stream)
+        for _ in range(steps):
+            fn()
+        e.record(stream)
+        torch.cuda.synchronize()
+        t = s.elapsed_time(e) * 1e-3 / steps
+        res[name] = {"K_per_s": nk / t, "ms": 1e3 * t}
+    if with_cpu:
+        ns = 5000
+        t0 = time.perf_counter()
+        oracle.soft_scattering(K[:ns], STANDARD_ROCK, MUON_MASS, threads=0)
+        res["soft_scattering"]["cpu_port_K_per_s"] = ns / (time.perf_counter() - t0)
+        t0 = time.perf_counter()
+        d = oracle.coulomb_data(K, STANDARD_ROCK, MUON_MASS)
+        Gc = oracle.coulomb_transport(d[1], d[2], 1.0)
+        oracle.hard_scattering(Gc, d[0], d[1], d[3], d[2])
+        res["coulomb_chain"]["cpu_port_K_per_s"] = nk / (time.perf_counter() - t0)
+        for v in (res["soft_scattering"], res["coulomb_chain"]):
+            v["speedup_vs_cpu"] = v["K_per_s"] / v["cpu_port_K_per_s"]
+    return res
+
+
 def time_surrogate(torch, args):
     """Learned surrogate (pair production, photonuclear): trained here on the
     GPU (plain-kernel data, tensor-core forward / backward, Adam; moderate
@@ -549,6 +609,7 @@ def run_ours(args):
         line["batched"] = time_batched(torch, args)
     if not args.no_integrals:
         line["recoil_integrals"] = time_integrals(torch, args, with_cpu=not args.no_cpu_baseline and world == 1)
+        line["transport"] = time_transport(torch, args, with_cpu=not args.no_cpu_baseline and world == 1)
     if not args.no_surrogate:
         line["surrogate"] = time_surrogate(torch, args)
     if not args.no_cpu_baseline and world == 1:

@@ -98,6 +98,41 @@ int noa_dcs_cuda_vmap(int process, int precision, double *result, const double *
 int noa_dcs_cuda_recoil_integral(int process, int moment, double *result, const double *K, int64_t n, double xlow,
                                  const noa_dcs_element *element, double mass, int32_t min_points, void *stream);
 
+/* Soft-scattering transverse transport per kinetic energy, the GPU form of
+ * dcs::soft_scattering (dcs.hh:941-952):
+ *   result[i] = transverse_transport_ionisation(K[i])      (dcs.hh:874-899)
+ *             + transverse_transport_photonuclear(K[i])    (dcs.hh:901-939),
+ * the latter a 102-node composite Gauss-Legendre rule over log(nu / 0.05) on
+ * [log 1e-6, 0] of the photonuclear DCS times its analytic angular weight.
+ * FP64; K and result are device buffers. */
+int noa_dcs_cuda_soft_scattering(double *result, const double *K, int64_t n, const noa_dcs_element *element,
+                                 double mass, void *stream);
+
+/* Elastic (Coulomb) scattering data per kinetic energy, the GPU form of
+ * dcs::coulomb_data (dcs.hh:604-622).  Outputs, in the reference's record
+ * layout: fCM [n][2] (CM Lorentz factors), screen [n][9] (three screening
+ * parameters and six pole-reduction factors), fspin [n], invlambda [n]
+ * (inverse Wentzel path).  FP64, device buffers. */
+int noa_dcs_cuda_coulomb_data(double *fCM, double *screen, double *fspin, double *invlambda, const double *K,
+                              int64_t n, const noa_dcs_element *element, double mass, void *stream);
+
+/* First two elastic transport coefficients below the cut-off angle mu, the
+ * GPU form of dcs::coulomb_transport (dcs.hh:679-699): coefficients [n][2]
+ * from screen [n][9] and fspin [n]; mu holds n_mu = 1 (one angle for all)
+ * or n values.  FP64, device buffers. */
+int noa_dcs_cuda_coulomb_transport(double *coefficients, const double *screen, const double *fspin,
+                                   const double *mu, int64_t n_mu, int64_t n, void *stream);
+
+/* Hard-scattering cut-off angle mu0 [nkin] and mean free path lb_h [nkin]
+ * over nel elements, the GPU form of dcs::hard_scattering (dcs.hh:840-872,
+ * Ridders' root of the restricted cross-section, numerics.hh:154-216).
+ * Inputs per element and energy: G [nel][nkin][2] (transport
+ * coefficients), fCM [nel][nkin][2], screen [nel][nkin][9], invlambda and
+ * fspin [nel][nkin].  FP64, device buffers. */
+int noa_dcs_cuda_hard_scattering(double *mu0, double *lb_h, const double *G, const double *fCM,
+                                 const double *screen, const double *invlambda, const double *fspin, int64_t nel,
+                                 int64_t nkin, void *stream);
+
 /* FP32-compensated form with an explicit tolerance: every pair whose
  * estimated relative error exceeds `tolerance` (0 < tolerance < 1) is
  * recomputed in FP64.  noa_dcs_cuda_vmap with NOA_DCS_FP32C uses 1e-6.

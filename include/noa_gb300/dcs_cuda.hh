@@ -40,8 +40,18 @@ struct AtomicElement {
 };
 using Energies = torch::Tensor;
 using Calculation = torch::Tensor;
+using Energy = Scalar;
 constexpr ParticleMass MUON_MASS = 0.10565839;
 constexpr AtomicElement STANDARD_ROCK = AtomicElement{22., 0.1364E-6, 11};
+namespace dcs {
+using InvLambdas = torch::Tensor;
+using ScreeningFactors = torch::Tensor;
+using FSpins = torch::Tensor;
+using CMLorentz = torch::Tensor;
+using AngularCutoff = torch::Tensor;
+using HSMeanFreePath = torch::Tensor;
+using TransportCoefs = torch::Tensor;
+} // namespace dcs
 } // namespace noa::pms
 #endif
 
@@ -72,4 +82,32 @@ Calculation map_ionisation(const Energies &kinetic_energies, const Energies &rec
 void vmap(int process, int precision, const Calculation &result, const Energies &kinetic_energies,
           const Energies &recoil_energies, const AtomicElement &element, const ParticleMass &mass);
 
+
+// GPU forms of the reference's per-K CPU functions (dcs.hh:89-130, 499-952),
+// same argument order; every tensor a contiguous float64 CUDA tensor.
+
+// dcs::vmap_integral(dcs::recoil_integral(dcs::<process>, del_integrand |
+// cel_integrand))(result, kinetic_energies, xlow, element, mass, min_points):
+// process 0..3 as in vmap, moment 0 = DEL, 1 = CEL.
+void recoil_integral(int process, int moment, const Calculation &result, const Energies &kinetic_energies,
+                     const Energy &xlow, const AtomicElement &element, const AtomicMass &mass, Index min_points);
+
+// dcs::soft_scattering(ms1, kinetic_energies, element, mass), dcs.hh:941-952.
+void soft_scattering(const Calculation &ms1, const Energies &kinetic_energies, const AtomicElement &element,
+                     const ParticleMass &mass);
+
+// dcs::coulomb_data, dcs.hh:600-622: fCM [n, 2], screening [n, 9], fspin [n], invlambda [n].
+void coulomb_data(const CMLorentz &fCM, const ScreeningFactors &screening, const FSpins &fspin,
+                  const InvLambdas &invlambda, const Energies &kinetic_energies, const AtomicElement &element,
+                  const ParticleMass &mass);
+
+// dcs::coulomb_transport, dcs.hh:674-699: coefficients [n, 2]; mu one value or [n].
+void coulomb_transport(const TransportCoefs &coefficients, const ScreeningFactors &screening, const FSpins &fspin,
+                       const AngularCutoff &mu);
+
+// dcs::hard_scattering, dcs.hh:842-872: invlambdas / fspins [nel, nkin],
+// coefficients / transform [nel, nkin, 2], screening [nel, nkin, 9].
+void hard_scattering(const AngularCutoff &mu0, const HSMeanFreePath &lb_h, const TransportCoefs &coefficients,
+                     const CMLorentz &transform, const ScreeningFactors &screening, const InvLambdas &invlambdas,
+                     const FSpins &fspins);
 } // namespace noa::pms::dcs::cuda

@@ -14,6 +14,8 @@ FP64, FP32C = 0, 1
 PRECISIONS = {"fp64": FP64, "fp32c": FP32C}
 
 SUCCESS = 0
+(ERROR_INVALID_VALUE, ERROR_INVALID_ELEMENT, ERROR_MISALIGNED, ERROR_NOT_DEVICE_MEMORY, ERROR_OVERLAP, ERROR_CUDA,
+ ERROR_TIMEOUT, ERROR_NOT_SUPPORTED) = range(1, 9)
 STATUS_NAMES = {
     0: "NOA_DCS_SUCCESS", 1: "NOA_DCS_ERROR_INVALID_VALUE", 2: "NOA_DCS_ERROR_INVALID_ELEMENT",
     3: "NOA_DCS_ERROR_MISALIGNED", 4: "NOA_DCS_ERROR_NOT_DEVICE_MEMORY", 5: "NOA_DCS_ERROR_OVERLAP",
@@ -50,6 +52,10 @@ SIGNATURES = {
     "noa_dcs_cuda_vmap_fp32c": (_INT, [_INT, _P, _P, _P, _I64, _EP, _D, ctypes.c_float, _P]),
     "noa_dcs_vmap_host": (_INT, [_INT, _INT, _P, _P, _P, _I64, _EP, _D]),
     "noa_dcs_cuda_recoil_integral": (_INT, [_INT, _INT, _P, _P, _I64, _D, _EP, _D, ctypes.c_int32, _P]),
+    "noa_dcs_cuda_soft_scattering": (_INT, [_P, _P, _I64, _EP, _D, _P]),
+    "noa_dcs_cuda_coulomb_data": (_INT, [_P, _P, _P, _P, _P, _I64, _EP, _D, _P]),
+    "noa_dcs_cuda_coulomb_transport": (_INT, [_P, _P, _P, _P, _I64, _I64, _P]),
+    "noa_dcs_cuda_hard_scattering": (_INT, [_P, _P, _P, _P, _P, _P, _P, _I64, _I64, _P]),
     "noa_dcs_release_staging": (_INT, []),
     "noa_dcs_status_string": (ctypes.c_char_p, [_INT]),
     "noa_dcs_last_error": (ctypes.c_char_p, []),

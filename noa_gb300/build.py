@@ -32,6 +32,12 @@ NVCC_FLAGS = ARCH + ["-O3", "-std=c++17", "-lineinfo", "--expt-relaxed-constexpr
                      "-Xcompiler", "-fPIC,-ffp-contract=off", "-I", os.path.join(ROOT, "include")]
 
 
+# Per-file extra flags.  coulomb.cu keeps the reference's IEEE operation
+# order (no FMA contraction): its Ridders iteration branches on signs of
+# differences, so contraction could change the iteration path.
+FILE_FLAGS = {"coulomb.cu": ["-fmad=false"]}
+
+
 def _nvcc():
     for cand in (shutil.which("nvcc"), "/usr/local/cuda/bin/nvcc"):
         if cand and os.path.exists(cand):
@@ -70,7 +76,8 @@ def build_cuda(verbose=False):
     objs = [os.path.join(BUILD, os.path.basename(s)[:-3] + ".o") for s in srcs]
     jobs = [(s, o) for s, o in zip(srcs, objs) if _stale(o, [s] + hdrs)]
     with cf.ThreadPoolExecutor(max_workers=max(1, min(len(jobs), os.cpu_count() or 4))) as ex:
-        outs = list(ex.map(lambda so: _run([nvcc] + NVCC_FLAGS + ["-c", so[0], "-o", so[1]]), jobs))
+        outs = list(ex.map(lambda so: _run([nvcc] + NVCC_FLAGS + FILE_FLAGS.get(os.path.basename(so[0]), []) +
+                                           ["-c", so[0], "-o", so[1]]), jobs))
     if verbose:
         for o in outs:
             sys.stdout.write(o)

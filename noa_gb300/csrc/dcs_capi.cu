@@ -18,7 +18,9 @@
 #include <cstdint>
 #include <cstdio>
 #include <cstring>
+#include <initializer_list>
 #include <mutex>
+#include <utility>
 
 namespace {
 
@@ -220,6 +222,113 @@ int noa_dcs_cuda_recoil_integral(int process, int moment, double *result, const 
     if (e != cudaSuccess)
         return cuda_fail(e, "recoil integral launch");
     return NOA_DCS_SUCCESS;
+}
+
+// ------------------------------------------------- per-K transport functions
+namespace {
+
+int current_device(int &device) {
+    const cudaError_t e = cudaGetDevice(&device);
+    return e == cudaSuccess ? NOA_DCS_SUCCESS : cuda_fail(e, "cudaGetDevice");
+}
+
+// Every named buffer must be device memory of the current device.
+int check_buffers(std::initializer_list<std::pair<const void *, const char *>> bufs) {
+    int device = 0, st;
+    if ((st = current_device(device)))
+        return st;
+    for (const auto &b : bufs)
+        if ((st = check_device_buffer(b.first, b.second, device)))
+            return st;
+    return NOA_DCS_SUCCESS;
+}
+
+int check_size_mass(int64_t n, double mass) {
+    if (n < 0)
+        return fail(NOA_DCS_ERROR_INVALID_VALUE, "negative size %lld", (long long)n);
+    if (!std::isfinite(mass) || !(mass > 0.))
+        return fail(NOA_DCS_ERROR_INVALID_VALUE, "invalid particle mass %g", mass);
+    return NOA_DCS_SUCCESS;
+}
+
+} // namespace
+
+int noa_dcs_cuda_soft_scattering(double *result, const double *K, int64_t n, const noa_dcs_element *element,
+                                 double mass, void *stream) {
+    g_last_error[0] = '\0';
+    int st;
+    if ((st = check_size_mass(n, mass)) || (st = check_element(element)))
+        return st;
+    if (n == 0)
+        return NOA_DCS_SUCCESS;
+    if ((st = check_buffers({{result, "result"}, {K, "K"}})))
+        return st;
+    if (overlaps_partially(result, K, n))
+        return fail(NOA_DCS_ERROR_OVERLAP, "result partially overlaps K");
+    noa_dcs_consts c;
+    noa_dcs_fill_consts(&c, element->A, element->I, element->Z, mass);
+    const cudaError_t e = noa_dcs_launch_soft_scattering(K, result, n, &c, (cudaStream_t)stream);
+    return e == cudaSuccess ? NOA_DCS_SUCCESS : cuda_fail(e, "soft scattering launch");
+}
+
+int noa_dcs_cuda_coulomb_data(double *fCM, double *screen, double *fspin, double *invlambda, const double *K,
+                              int64_t n, const noa_dcs_element *element, double mass, void *stream) {
+    g_last_error[0] = '\0';
+    int st;
+    if ((st = check_size_mass(n, mass)) || (st = check_element(element)))
+        return st;
+    if (n == 0)
+        return NOA_DCS_SUCCESS;
+    if ((st = check_buffers({{fCM, "fCM"}, {screen, "screen"}, {fspin, "fspin"}, {invlambda, "invlambda"},
+                             {K, "K"}})))
+        return st;
+    noa_coulomb_element e;
+    e.A = element->A;
+    e.A13 = std::pow(element->A, 1. / 3);  // dcs.hh:545-546
+    e.Z23 = std::pow((double)element->Z, 2. / 3.);  // dcs.hh:589
+    e.Z = element->Z;
+    const cudaError_t ce = noa_dcs_launch_coulomb_data(K, n, &e, mass, fCM, screen, fspin, invlambda,
+                                                       (cudaStream_t)stream);
+    return ce == cudaSuccess ? NOA_DCS_SUCCESS : cuda_fail(ce, "coulomb data launch");
+}
+
+int noa_dcs_cuda_coulomb_transport(double *coefficients, const double *screen, const double *fspin,
+                                   const double *mu, int64_t n_mu, int64_t n, void *stream) {
+    g_last_error[0] = '\0';
+    if (n < 0)
+        return fail(NOA_DCS_ERROR_INVALID_VALUE, "negative size %lld", (long long)n);
+    if (n == 0)
+        return NOA_DCS_SUCCESS;
+    if (n_mu != 1 && n_mu != n)
+        return fail(NOA_DCS_ERROR_INVALID_VALUE, "mu must hold 1 or n = %lld values, got %lld", (long long)n,
+                    (long long)n_mu);
+    int st;
+    if ((st = check_buffers({{coefficients, "coefficients"}, {screen, "screen"}, {fspin, "fspin"}, {mu, "mu"}})))
+        return st;
+    const cudaError_t e =
+        noa_dcs_launch_coulomb_transport(screen, fspin, mu, n_mu, n, coefficients, (cudaStream_t)stream);
+    return e == cudaSuccess ? NOA_DCS_SUCCESS : cuda_fail(e, "coulomb transport launch");
+}
+
+int noa_dcs_cuda_hard_scattering(double *mu0, double *lb_h, const double *G, const double *fCM,
+                                 const double *screen, const double *invlambda, const double *fspin, int64_t nel,
+                                 int64_t nkin, void *stream) {
+    g_last_error[0] = '\0';
+    if (nkin < 0 || nel < 1)
+        return fail(NOA_DCS_ERROR_INVALID_VALUE, "need nel >= 1 and nkin >= 0, got %lld, %lld", (long long)nel,
+                    (long long)nkin);
+    if (nkin == 0)
+        return NOA_DCS_SUCCESS;
+    int st;
+    if ((st = check_buffers({{mu0, "mu0"}, {lb_h, "lb_h"}, {G, "G"}, {fCM, "fCM"}, {screen, "screen"},
+                             {invlambda, "invlambda"}, {fspin, "fspin"}})))
+        return st;
+    if (mu0 == lb_h || overlaps_partially(mu0, lb_h, nkin))
+        return fail(NOA_DCS_ERROR_OVERLAP, "mu0 and lb_h overlap");
+    const double max_mu0 = 0.5 * (1. - std::cos(1E+00 * M_PI / 180.));  // physics.hh:81-84
+    const cudaError_t e = noa_dcs_launch_hard_scattering(G, fCM, screen, invlambda, fspin, nel, nkin, max_mu0, mu0,
+                                                         lb_h, (cudaStream_t)stream);
+    return e == cudaSuccess ? NOA_DCS_SUCCESS : cuda_fail(e, "hard scattering launch");
 }
 
 int noa_dcs_vmap_host(int process, int precision, double *result, const double *K, const double *q, int64_t n,

@@ -218,6 +218,154 @@ __global__ void __launch_bounds__(I_THREADS) recoil_integral_kernel(const Integr
     }
 }
 
+// ------------------------------------------------ soft-scattering transport
+/*
+ * soft_scattering (dcs.hh:941-952) per K: the closed-form ionisation part
+ * (dcs.hh:874-899) plus twice a 6-node composite GL rule over
+ * t = log(nu / X_FRACTION) on [log 1e-6, 0] with 17 intervals (102 nodes) of
+ * photonuclear(K, q) * ratio(K, q) * nu, q = nu K, where ratio is the
+ * mu-integrated angular weight of dcs.hh:911-934.  Same tile / queue scheme
+ * as the recoil integrals: closed photonuclear nodes contribute
+ * 0 * ratio * nu (0, or NaN where the weight is not finite, as in the
+ * reference), open ones are evaluated 256 at a time.
+ */
+constexpr int S_NODES = 102;            // 6 * ceil(100 / 6)
+constexpr int S_KPT = I_PAIRS / S_NODES; // 15 kinetic energies per tile
+constexpr int S_PAIRS = S_KPT * S_NODES;
+
+struct SoftParams {
+    const double *K;
+    double *out;
+    int64_t n;
+    double lb;  // log(1e-6)
+    double h;   // -lb / 17
+};
+
+// dcs.hh:913-934 in the reference's operation order.
+__device__ __forceinline__ double soft_ratio(double K, double q, double mass) {
+    const double E = x_add(K, mass);
+    const double m02 = 0.4;
+    const double q2 = x_mul(q, q);
+    const double tmax = x_mul(1.876544, q);
+    const double tmin = x_div(x_mul(x_mul(q2, mass), mass), x_mul(E, x_sub(E, q)));
+    const double b1 = x_div(1., x_sub(1., x_div(q2, m02)));
+    const double c1 = x_div(1., x_sub(1., x_div(m02, q2)));
+    double L1 = x_mul(b1, log(x_div(x_add(q2, tmax), x_add(q2, tmin))));
+    double L2 = x_mul(c1, log(x_div(x_add(m02, tmax), x_add(m02, tmin))));
+    const double I0 = x_sub(x_sub(log(x_div(tmax, tmin)), L1), L2);
+    L1 = x_mul(L1, q2);
+    L2 = x_mul(L2, m02);
+    const double I1 = x_add(L1, L2);
+    L1 = x_mul(L1, q2);
+    L2 = x_mul(L2, m02);
+    const double I2 = x_sub(x_sub(x_mul(x_sub(tmax, tmin), x_add(x_mul(b1, q2), x_mul(c1, m02))), L1), L2);
+    return x_div(x_sub(x_mul(I1, tmax), I2),
+                 x_mul(x_mul(x_sub(x_mul(I0, tmax), I1), K), x_add(K, x_mul(2., mass))));
+}
+
+// dcs.hh:874-899 in the reference's operation order.
+__device__ __forceinline__ double soft_ionisation(double K, const noa_dcs_consts &c) {
+    const double mass = c.mass;
+    const double p2 = x_mul(K, x_add(K, x_mul(2., mass)));
+    const double E = x_add(K, mass);
+    const double Wmax = x_div(x_mul(x_mul(2., ME), p2), x_add(x_mul(mass, mass), x_mul(ME, x_add(ME, x_mul(2., E)))));
+    const double W0 = x_div(x_mul(2., p2), ME);
+    const double mu_max = x_div(Wmax, W0);
+    double mu3 = x_div(x_mul(K, NOA_X_FRACTION), W0);
+    if (mu3 > mu_max)
+        mu3 = mu_max;
+    const double mu2 = x_div(x_mul(0.62, c.I), W0);
+    if (mu2 >= mu3)
+        return 0.;
+    const double a0 = x_div(x_mul(0.5, W0), p2);
+    const double a1 = x_div(-1., Wmax);
+    const double a2 = x_div(x_mul(E, E), x_mul(W0, p2));
+    const double cs0 = x_div(1.535336E-05, c.A);
+    const double bracket = x_add(x_add(x_mul(x_mul(0.5, a0), x_sub(x_mul(mu3, mu3), x_mul(mu2, mu2))),
+                                       x_mul(a1, x_sub(mu3, mu2))),
+                                 x_mul(a2, log(x_div(mu3, mu2))));
+    return x_mul(x_mul(x_mul(2., cs0), c.Zd), bracket);
+}
+
+// Node i of the rule for kinetic energy K: nu and q (numerics.hh:84-86, dcs.hh:910-911).
+__device__ __forceinline__ void soft_node(double K, int i, const SoftParams &p, double &nu, double &q) {
+    const double t = x_add(p.lb, x_mul(p.h, (double)(i / 6) + kGL6X[i % 6]));
+    nu = x_mul(NOA_X_FRACTION, exp(t));
+    q = x_mul(nu, K);
+}
+
+__global__ void __launch_bounds__(I_THREADS) soft_scattering_kernel(const SoftParams p, const noa_dcs_consts c) {
+    __shared__ double vals[S_PAIRS];
+    __shared__ int qS[S_PAIRS + I_THREADS];
+    __shared__ double sK[S_KPT];
+    __shared__ int warp_tot[I_THREADS / 32];
+    __shared__ int tile_open;
+    const int64_t tiles = (p.n + S_KPT - 1) / S_KPT;
+
+    for (int64_t tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
+        const int64_t k0 = tile * S_KPT;
+        if ((int)threadIdx.x < S_KPT) {
+            const int64_t ki = k0 + threadIdx.x;
+            sK[threadIdx.x] = ki < p.n ? p.K[ki] : 1.;
+        }
+        __syncthreads();
+        int qn = 0;
+        for (int base = 0; base < S_PAIRS; base += I_THREADS) {
+            const int slot = base + threadIdx.x;
+            bool open = false;
+            if (slot < S_PAIRS) {
+                const int kk = slot / S_NODES, i = slot - kk * S_NODES;
+                vals[slot] = 0.;
+                if (k0 + kk < p.n) {
+                    const double K = sK[kk];
+                    double nu, q;
+                    soft_node(K, i, p, nu, q);
+                    open = photo_live(K, q, c);
+                    if (!open)  // photonuclear = 0: 0 * ratio * nu * h * w
+                        vals[slot] = x_mul(x_mul(x_mul(x_mul(0., soft_ratio(K, q, c.mass)), nu), p.h), kGL6W[i % 6]);
+                }
+            }
+            const int pos = qn + i_scan(open ? 1 : 0, warp_tot, &tile_open);
+            if (open)
+                qS[pos] = slot;
+            __syncthreads();
+            qn += tile_open;
+            while (qn >= I_THREADS) {
+                const int sl = qS[qn - I_THREADS + threadIdx.x];
+                const int kk = sl / S_NODES, i = sl - kk * S_NODES;
+                const double K = sK[kk];
+                double nu, q;
+                soft_node(K, i, p, nu, q);
+                const double f = x_mul(x_mul(photo_fp64(K, q, c), soft_ratio(K, q, c.mass)), nu);
+                vals[sl] = x_mul(x_mul(f, p.h), kGL6W[i % 6]);
+                qn -= I_THREADS;
+                __syncthreads();
+            }
+        }
+        if ((int)threadIdx.x < qn) {
+            const int sl = qS[threadIdx.x];
+            const int kk = sl / S_NODES, i = sl - kk * S_NODES;
+            const double K = sK[kk];
+            double nu, q;
+            soft_node(K, i, p, nu, q);
+            const double f = x_mul(x_mul(photo_fp64(K, q, c), soft_ratio(K, q, c.mass)), nu);
+            vals[sl] = x_mul(x_mul(f, p.h), kGL6W[i % 6]);
+        }
+        __syncthreads();
+        if ((int)threadIdx.x < S_KPT) {
+            const int64_t ki = k0 + threadIdx.x;
+            if (ki < p.n) {
+                double s = 0.;
+                const double *v = vals + threadIdx.x * S_NODES;
+                for (int i = 0; i < S_NODES; i++)
+                    s = x_add(s, v[i]);
+                p.out[ki] = x_add(soft_ionisation(sK[threadIdx.x], c), x_mul(2., s));
+            }
+        }
+        __syncthreads();
+    }
+}
+
 static int sm_count() {
     int dev = 0, sms = 0;
     cudaGetDevice(&dev);
@@ -266,5 +414,22 @@ cudaError_t noa_dcs_launch_recoil_integral(int process, int moment, const double
     default:
         return cudaErrorInvalidValue;
     }
+    return cudaGetLastError();
+}
+
+cudaError_t noa_dcs_launch_soft_scattering(const double *K, double *out, int64_t n, const noa_dcs_consts *c,
+                                           cudaStream_t stream) {
+    if (n <= 0)
+        return cudaSuccess;
+    SoftParams p;
+    p.K = K;
+    p.out = out;
+    p.n = n;
+    p.lb = log(1E-06);                // dcs.hh:905
+    p.h = (0. - p.lb) / (double)17u;  // numerics.hh:80-81, n_itv = ceil(100 / 6)
+    const int64_t tiles = (n + S_KPT - 1) / S_KPT;
+    const int64_t cap = (int64_t)sm_count() * 3;
+    const int grid = (int)(tiles < cap ? tiles : cap);
+    soft_scattering_kernel<<<grid, I_THREADS, 0, stream>>>(p, *c);
     return cudaGetLastError();
 }

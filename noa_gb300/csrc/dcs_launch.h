@@ -43,3 +43,26 @@ int noa_dcs_batched_occupancy32(int process, int threads, size_t smem);
 cudaError_t noa_dcs_launch_recoil_integral(int process, int moment, const double *K, double *out, int64_t n,
                                            double xlow, int min_points, const noa_dcs_consts *c,
                                            cudaStream_t stream);
+
+/* Soft-scattering transverse transport per K (dcs_integral.cu). */
+cudaError_t noa_dcs_launch_soft_scattering(const double *K, double *out, int64_t n, const noa_dcs_consts *c,
+                                           cudaStream_t stream);
+
+/* Per-element constants of the elastic-scattering kernels, computed on the
+ * host with the C library: A13 = pow(A, 1/3), Z23 = pow(Z, 2/3). */
+struct noa_coulomb_element {
+    double A;
+    double A13;
+    double Z23;
+    int32_t Z;
+};
+
+/* Elastic scattering (coulomb.cu).  Arguments are already validated. */
+cudaError_t noa_dcs_launch_coulomb_data(const double *K, int64_t n, const noa_coulomb_element *e, double mass,
+                                        double *fCM, double *screen, double *fspin, double *invlambda,
+                                        cudaStream_t stream);
+cudaError_t noa_dcs_launch_coulomb_transport(const double *screen, const double *fspin, const double *mu,
+                                             int64_t n_mu, int64_t n, double *coefs, cudaStream_t stream);
+cudaError_t noa_dcs_launch_hard_scattering(const double *G, const double *fCM, const double *screen,
+                                           const double *invlambda, const double *fspin, int64_t nel, int64_t nkin,
+                                           double max_mu0, double *mu0, double *lb_h, cudaStream_t stream);

@@ -18,7 +18,8 @@ from . import _lib
 from .elements import MUON_MASS, STANDARD_ROCK, X_FRACTION, AtomicElement
 
 __all__ = [
-    "vmap", "map", "vmap_host", "recoil_integral",
+    "vmap", "map", "vmap_host", "recoil_integral", "soft_scattering",
+    "coulomb_data", "coulomb_transport", "hard_scattering",
     "vmap_bremsstrahlung", "vmap_pair_production", "vmap_photonuclear", "vmap_ionisation",
     "map_bremsstrahlung", "map_pair_production", "map_photonuclear", "map_ionisation",
 ]
@@ -108,6 +109,86 @@ def recoil_integral(process, moment, result, kinetic_energies, xlow=X_FRACTION, 
                                                     kinetic_energies.data_ptr(), n, float(xlow), el, float(mass),
                                                     int(min_points), stream))
     return result
+
+
+def _stream(t):
+    return torch.cuda.current_stream(t.device).cuda_stream
+
+
+def soft_scattering(ms1, kinetic_energies, element=STANDARD_ROCK, mass=MUON_MASS):
+    """GPU form of dcs::soft_scattering (dcs.hh:941-952): ms1[i] = the
+    transverse-transport coefficient of ionisation + photonuclear at
+    kinetic_energies[i]."""
+    lib = _lib.load()
+    _check_tensor(ms1, "ms1")
+    _check_tensor(kinetic_energies, "kinetic_energies", ms1.device)
+    n = ms1.numel()
+    if kinetic_energies.numel() != n:
+        raise RuntimeError("size mismatch")
+    with torch.cuda.device(ms1.device):
+        _lib.check(lib.noa_dcs_cuda_soft_scattering(ms1.data_ptr(), kinetic_energies.data_ptr(), n,
+                                                    _lib.element_struct(element), float(mass), _stream(ms1)))
+    return ms1
+
+
+def coulomb_data(fCM, screening, fspin, invlambda, kinetic_energies, element=STANDARD_ROCK, mass=MUON_MASS):
+    """GPU form of dcs::coulomb_data (dcs.hh:604-622), same argument order:
+    fills fCM [n, 2], screening [n, 9], fspin [n] and invlambda [n]."""
+    lib = _lib.load()
+    _check_tensor(kinetic_energies, "kinetic_energies")
+    dev = kinetic_energies.device
+    n = kinetic_energies.numel()
+    for t, name, width in ((fCM, "fCM", 2), (screening, "screening", 9), (fspin, "fspin", 1),
+                           (invlambda, "invlambda", 1)):
+        _check_tensor(t, name, dev)
+        if t.numel() != width * n:
+            raise RuntimeError(f"{name} must hold {width} x {n} values")
+    with torch.cuda.device(dev):
+        _lib.check(lib.noa_dcs_cuda_coulomb_data(fCM.data_ptr(), screening.data_ptr(), fspin.data_ptr(),
+                                                 invlambda.data_ptr(), kinetic_energies.data_ptr(), n,
+                                                 _lib.element_struct(element), float(mass), _stream(fCM)))
+
+
+def coulomb_transport(coefficients, screening, fspin, mu):
+    """GPU form of dcs::coulomb_transport (dcs.hh:679-699): coefficients
+    [n, 2] below the cut-off angle mu (one value, or one per energy)."""
+    lib = _lib.load()
+    _check_tensor(fspin, "fspin")
+    dev = fspin.device
+    n = fspin.numel()
+    _check_tensor(coefficients, "coefficients", dev)
+    _check_tensor(screening, "screening", dev)
+    _check_tensor(mu, "mu", dev)
+    if coefficients.numel() != 2 * n or screening.numel() != 9 * n or mu.numel() not in (1, n):
+        raise RuntimeError("size mismatch")
+    with torch.cuda.device(dev):
+        _lib.check(lib.noa_dcs_cuda_coulomb_transport(coefficients.data_ptr(), screening.data_ptr(),
+                                                      fspin.data_ptr(), mu.data_ptr(), mu.numel(), n,
+                                                      _stream(fspin)))
+
+
+def hard_scattering(mu0, lb_h, coefficients, transform, screening, invlambdas, fspins):
+    """GPU form of dcs::hard_scattering (dcs.hh:840-872), same argument
+    order: mu0 and lb_h [nkin] from per-element inputs shaped like the
+    reference's, invlambdas and fspins [nel, nkin], coefficients and
+    transform [nel, nkin, 2], screening [nel, nkin, 9]."""
+    lib = _lib.load()
+    _check_tensor(invlambdas, "invlambdas")
+    dev = invlambdas.device
+    if invlambdas.dim() != 2:
+        raise RuntimeError("invlambdas must be [nel, nkin]")
+    nel, nkin = invlambdas.shape
+    for t, name, width in ((mu0, "mu0", 1), (lb_h, "lb_h", 1), (coefficients, "coefficients", 2 * nel),
+                           (transform, "transform", 2 * nel), (screening, "screening", 9 * nel),
+                           (fspins, "fspins", nel)):
+        _check_tensor(t, name, dev)
+        if t.numel() != width * nkin:
+            raise RuntimeError(f"{name} must hold {width} x {nkin} values")
+    with torch.cuda.device(dev):
+        _lib.check(lib.noa_dcs_cuda_hard_scattering(mu0.data_ptr(), lb_h.data_ptr(), coefficients.data_ptr(),
+                                                    transform.data_ptr(), screening.data_ptr(),
+                                                    invlambdas.data_ptr(), fspins.data_ptr(), nel, nkin,
+                                                    _stream(mu0)))
 
 
 def _bind(pid):

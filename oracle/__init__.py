@@ -48,8 +48,20 @@ def lib():
         L.oracle_dcs_opcount.argtypes = [_INT, _P, _P, _I64, _D, _D, _I32, _D, _P]
         L.oracle_dcs_opcount.restype = _D
         L.oracle_max_threads.restype = _INT
+        _elastic_signatures(L, "oracle")
+        L.oracle_soft_scattering.argtypes = [_P, _P, _I64, _D, _D, _I32, _D, _INT]
+        L.oracle_soft_scattering.restype = _INT
         _oracle = L
     return _oracle
+
+
+def _elastic_signatures(L, prefix):
+    for name, args in (("coulomb_data", [_P, _I64, _D, _D, _I32, _D, _P, _P, _P, _P]),
+                       ("coulomb_transport", [_P, _P, _P, _I64, _I64, _P]),
+                       ("hard_scattering", [_P, _P, _P, _P, _P, _I64, _I64, _P, _P])):
+        f = getattr(L, f"{prefix}_{name}")
+        f.argtypes = args
+        f.restype = _INT
 
 
 def ref_available():
@@ -66,6 +78,9 @@ def ref_lib():
         L.ref_dcs_vmap.restype = _INT
         L.ref_recoil_integral_vmap.argtypes = [_INT, _INT, _P, _P, _I64, _D, _D, _D, _I32, _D, _I32]
         L.ref_recoil_integral_vmap.restype = _INT
+        _elastic_signatures(L, "ref")
+        L.ref_soft_scattering.argtypes = [_P, _P, _I64, _D, _D, _I32, _D]
+        L.ref_soft_scattering.restype = _INT
         _ref = L
     return _ref
 
@@ -122,6 +137,85 @@ def ref_recoil_integral(process, moment, K, xlow, element, mass, min_points=180)
                                             int(min_points))
     if rc:
         raise ValueError(f"ref_recoil_integral_vmap failed ({rc})")
+    return out
+
+
+def _coulomb_data(L, prefix, K, element, mass):
+    K = _f64(K)
+    n = K.size
+    fCM, screen = np.empty((n, 2)), np.empty((n, 9))
+    fspin, invlambda = np.empty(n), np.empty(n)
+    getattr(L, f"{prefix}_coulomb_data")(_ptr(K), n, float(element.A), float(element.I), int(element.Z),
+                                          float(mass), _ptr(fCM), _ptr(screen), _ptr(fspin), _ptr(invlambda))
+    return fCM, screen, fspin, invlambda
+
+
+def _coulomb_transport(L, prefix, screen, fspin, mu):
+    screen, fspin, mu = _f64(screen), _f64(fspin), _f64(np.atleast_1d(mu))
+    n = fspin.size
+    if mu.size not in (1, n):
+        raise ValueError("mu must hold 1 or len(fspin) values")
+    coefs = np.empty((n, 2))
+    getattr(L, f"{prefix}_coulomb_transport")(_ptr(screen), _ptr(fspin), _ptr(mu), mu.size, n, _ptr(coefs))
+    return coefs
+
+
+def _hard_scattering(L, prefix, G, fCM, screen, invlambda, fspin):
+    invlambda = _f64(invlambda)
+    if invlambda.ndim == 1:
+        invlambda = invlambda[None]
+    nel, nkin = invlambda.shape
+    G, fCM, screen, fspin = (_f64(a) for a in (G, fCM, screen, fspin))
+    if G.size != 2 * nel * nkin or fCM.size != 2 * nel * nkin or screen.size != 9 * nel * nkin \
+            or fspin.size != nel * nkin:
+        raise ValueError("hard_scattering: inconsistent shapes")
+    mu0, lb_h = np.empty(nkin), np.empty(nkin)
+    getattr(L, f"{prefix}_hard_scattering")(_ptr(G), _ptr(fCM), _ptr(screen), _ptr(invlambda), _ptr(fspin), nel,
+                                            nkin, _ptr(mu0), _ptr(lb_h))
+    return mu0, lb_h
+
+
+def coulomb_data(K, element, mass):
+    """Oracle coulomb_data (dcs.hh:604-622): (fCM [n,2], screen [n,9], fspin, invlambda)."""
+    return _coulomb_data(lib(), "oracle", K, element, mass)
+
+
+def coulomb_transport(screen, fspin, mu):
+    """Oracle coulomb_transport (dcs.hh:679-699): coefficients [n,2]; mu scalar or [n]."""
+    return _coulomb_transport(lib(), "oracle", screen, fspin, mu)
+
+
+def hard_scattering(G, fCM, screen, invlambda, fspin):
+    """Oracle hard_scattering (dcs.hh:840-872) over [nel, nkin] inputs: (mu0, lb_h)."""
+    return _hard_scattering(lib(), "oracle", G, fCM, screen, invlambda, fspin)
+
+
+def soft_scattering(K, element, mass, threads=0):
+    """Oracle soft_scattering (dcs.hh:941-952) per K."""
+    K = _f64(K)
+    out = np.empty_like(K)
+    lib().oracle_soft_scattering(_ptr(K), _ptr(out), K.size, float(element.A), float(element.I), int(element.Z),
+                                 float(mass), int(threads))
+    return out
+
+
+def ref_coulomb_data(K, element, mass):
+    return _coulomb_data(ref_lib(), "ref", K, element, mass)
+
+
+def ref_coulomb_transport(screen, fspin, mu):
+    return _coulomb_transport(ref_lib(), "ref", screen, fspin, mu)
+
+
+def ref_hard_scattering(G, fCM, screen, invlambda, fspin):
+    return _hard_scattering(ref_lib(), "ref", G, fCM, screen, invlambda, fspin)
+
+
+def ref_soft_scattering(K, element, mass):
+    K = _f64(K)
+    out = np.empty_like(K)
+    ref_lib().ref_soft_scattering(_ptr(K), _ptr(out), K.size, float(element.A), float(element.I), int(element.Z),
+                                  float(mass))
     return out
 
 

@@ -12,6 +12,7 @@
  * tests and by the CPU baseline of bench.py through ctypes.  The product
  * library never links it.
  */
+#include "coulomb_oracle.hpp"
 #include "dcs_oracle.hpp"
 
 #include <omp.h>
@@ -61,6 +62,49 @@ int oracle_recoil_integral_vmap(int process, int moment, const double *K, double
 }
 
 int oracle_max_threads(void) { return omp_get_max_threads(); }
+
+/* Elastic scattering per kinetic energy (coulomb_data, dcs.hh:604-622):
+ * fCM [n][2], screen [n][9], fspin [n], invlambda [n]. */
+int oracle_coulomb_data(const double *K, int64_t n, double A, double I, int32_t Z, double mass, double *fCM,
+                        double *screen, double *fspin, double *invlambda) {
+    const Element el{A, I, Z};
+    for (int64_t i = 0; i < n; i++)
+        coulomb_data(fCM + 2 * i, screen + NSF * i, fspin + i, invlambda + i, K[i], el, mass);
+    return 0;
+}
+
+/* Transport coefficients (coulomb_transport, dcs.hh:679-699): coefs [n][2];
+ * mu holds n_mu = 1 (shared) or n values. */
+int oracle_coulomb_transport(const double *screen, const double *fspin, const double *mu, int64_t n_mu, int64_t n,
+                             double *coefs) {
+    for (int64_t i = 0; i < n; i++)
+        coulomb_transport_coefficients(coefs + 2 * i, screen + NSF * i, fspin[i], mu[n_mu == 1 ? 0 : i]);
+    return 0;
+}
+
+/* Hard-scattering cut-off and path (hard_scattering, dcs.hh:840-872) over
+ * nel elements x nkin energies: G, fCM [nel][nkin][2], screen
+ * [nel][nkin][9], invlambda, fspin [nel][nkin]; mu0, lb_h [nkin]. */
+int oracle_hard_scattering(const double *G, const double *fCM, const double *screen, const double *invlambda,
+                           const double *fspin, int64_t nel, int64_t nkin, double *mu0, double *lb_h) {
+    for (int64_t i = 0; i < nkin; i++)
+        coulomb_hard_scattering(mu0[i], lb_h[i], G + 2 * i, fCM + 2 * i, screen + NSF * i, invlambda + i,
+                                fspin + i, nel, nkin);
+    return 0;
+}
+
+/* Soft-scattering transverse transport per kinetic energy (soft_scattering,
+ * dcs.hh:941-952).  Same threading rule as oracle_dcs_vmap. */
+int oracle_soft_scattering(const double *K, double *out, int64_t n, double A, double I, int32_t Z, double mass,
+                           int threads) {
+    const Element el{A, I, Z};
+    const int nt = threads <= 0 ? omp_get_max_threads() : threads;
+#pragma omp parallel for schedule(static) num_threads(nt) if (threads != 1)
+    for (int64_t i = 0; i < n; i++)
+        out[i] = soft_scattering(K[i], el, mass);
+    return 0;
+}
+
 
 /* Operation counts, accumulated over the n pairs by oracle_dcs_opcount.
  * Exported in this layout: add, mul, div, sqrt, cmp, transcendental. */

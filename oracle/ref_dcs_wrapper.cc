@@ -6,7 +6,9 @@
  * lie (include path <noa checkout>/src) and the pip LibTorch, into
  * oracle/_ref/libnoa_ref_dcs.so.  It calls the reference's own dcs::vmap /
  * dcs::pvmap (dcs.hh:35-75) and dcs::vmap_integral(dcs::recoil_integral(...))
- * (dcs.hh:89-130) on tensors that wrap the caller's buffers, so the golden
+ * (dcs.hh:89-130), the elastic-scattering functions coulomb_data,
+ * coulomb_transport and hard_scattering (dcs.hh:604-872) and soft_scattering
+ * (dcs.hh:941-952) on tensors that wrap the caller's buffers, so the golden
  * vectors under tests/golden come from the reference code path itself.
  */
 #include <noa/pms/dcs.hh>
@@ -15,6 +17,7 @@
 #include <torch/torch.h>
 
 #include <cstdint>
+#include <vector>
 
 using namespace noa::pms;
 
@@ -91,4 +94,40 @@ int ref_recoil_integral_vmap(int process, int moment, const double *K, double *o
         return -1;
     }
 }
+
+int ref_coulomb_data(const double *K, int64_t n, double A, double I, int32_t Z, double mass, double *fCM,
+                     double *screen, double *fspin, double *invlambda) {
+    const AtomicElement el{A, I, Z};
+    auto o = torch::TensorOptions().dtype(torch::kFloat64);
+    dcs::coulomb_data(torch::from_blob(fCM, {n, 2}, o), torch::from_blob(screen, {n, 9}, o), wrap(fspin, n),
+                      wrap(invlambda, n), wrap(K, n), el, mass);
+    return 0;
 }
+
+int ref_coulomb_transport(const double *screen, const double *fspin, const double *mu, int64_t n_mu, int64_t n,
+                          double *coefs) {
+    auto o = torch::TensorOptions().dtype(torch::kFloat64);
+    auto tmu = n_mu == 1 ? torch::from_blob(const_cast<double *>(mu), {}, o) : wrap(mu, n);
+    dcs::coulomb_transport(torch::from_blob(coefs, {n, 2}, o),
+                           torch::from_blob(const_cast<double *>(screen), {n, 9}, o), wrap(fspin, n), tmu);
+    return 0;
+}
+
+int ref_hard_scattering(const double *G, const double *fCM, const double *screen, const double *invlambda,
+                        const double *fspin, int64_t nel, int64_t nkin, double *mu0, double *lb_h) {
+    auto o = torch::TensorOptions().dtype(torch::kFloat64);
+    auto blob = [&](const double *p, std::vector<int64_t> shape) {
+        return torch::from_blob(const_cast<double *>(p), shape, o);
+    };
+    dcs::hard_scattering(wrap(mu0, nkin), wrap(lb_h, nkin), blob(G, {nel, nkin, 2}), blob(fCM, {nel, nkin, 2}),
+                         blob(screen, {nel, nkin, 9}), blob(invlambda, {nel, nkin}), blob(fspin, {nel, nkin}));
+    return 0;
+}
+
+int ref_soft_scattering(const double *K, double *out, int64_t n, double A, double I, int32_t Z, double mass) {
+    const AtomicElement el{A, I, Z};
+    dcs::soft_scattering(wrap(out, n), wrap(K, n), el, mass);
+    return 0;
+}
+}
+

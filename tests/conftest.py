@@ -9,6 +9,7 @@ if ROOT not in sys.path:
     sys.path.insert(0, ROOT)
 
 GOLDEN = os.path.join(ROOT, "tests", "golden", "dcs_golden.npz")
+ELASTIC_GOLDEN = os.path.join(ROOT, "tests", "golden", "elastic_golden.npz")
 
 
 def pytest_configure(config):
@@ -25,6 +26,12 @@ def built():
 @pytest.fixture(scope="session")
 def golden():
     with np.load(GOLDEN) as z:
+        return {k: z[k] for k in z.files}
+
+
+@pytest.fixture(scope="session")
+def elastic_golden():
+    with np.load(ELASTIC_GOLDEN) as z:
         return {k: z[k] for k in z.files}
 
 

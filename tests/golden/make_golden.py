@@ -18,6 +18,12 @@ dcs::vmap_integral(dcs::recoil_integral(...)) on
 
 and stores inputs and outputs.  The fixtures pin the CPU oracle (bit for bit)
 and the CUDA kernels (to the stated tolerance) on hosts without the checkout.
+
+A second file, elastic_golden.npz, holds the reference's elastic-scattering
+and transverse-transport outputs (dcs::coulomb_data, coulomb_transport,
+hard_scattering, soft_scattering, dcs.hh:499-952) on a log grid of kinetic
+energies, seeded energies and the kinematic edges of those functions, for the
+same three elements, plus hard scattering over the three elements at once.
 """
 import json
 import os
@@ -111,5 +117,43 @@ def main():
     print(path, os.path.getsize(path), "bytes", len(out), "arrays")
 
 
+def elastic_energies():
+    """Kinetic energies for the elastic fixtures: a log grid over
+    [1e-6, 1e6] GeV, seeded energies, and points around the switches of
+    coulomb_screening_parameters (zeta2 = 1 moves with Z and K)."""
+    grid = np.logspace(-6, 6, 193)
+    seeded, _ = kinetic_recoil(N_INTEGRAL, offset=N_SEEDED)
+    return np.concatenate([grid, seeded, [1e-9, 1e-7, 0.1, 0.2, 0.5]])
+
+
+def elastic():
+    out = {}
+    K = elastic_energies()
+    out["K"] = K
+    mu_var = np.logspace(-25, 0, K.size)
+    stack = {name: [] for name in ("fCM", "screen", "fspin", "invlambda", "G")}
+    for ename, el in GOLDEN_ELEMENTS.items():
+        fCM, screen, fspin, invlambda = oracle.ref_coulomb_data(K, el, MUON_MASS)
+        out[f"{ename}_fCM"], out[f"{ename}_screen"] = fCM, screen
+        out[f"{ename}_fspin"], out[f"{ename}_invlambda"] = fspin, invlambda
+        G = oracle.ref_coulomb_transport(screen, fspin, 1.0)
+        out[f"{ename}_G"] = G
+        out[f"{ename}_G_mu"] = oracle.ref_coulomb_transport(screen, fspin, mu_var)
+        out[f"{ename}_mu0"], out[f"{ename}_lb_h"] = oracle.ref_hard_scattering(G, fCM, screen, invlambda, fspin)
+        out[f"{ename}_soft"] = oracle.ref_soft_scattering(K, el, MUON_MASS)
+        for name, v in zip(("fCM", "screen", "fspin", "invlambda", "G"), (fCM, screen, fspin, invlambda, G)):
+            stack[name].append(v)
+    st = {k: np.stack(v) for k, v in stack.items()}
+    out["all_mu0"], out["all_lb_h"] = oracle.ref_hard_scattering(st["G"], st["fCM"], st["screen"],
+                                                                 st["invlambda"], st["fspin"])
+    out["mu_var"] = mu_var
+    out["meta"] = np.array(json.dumps({"mass": MUON_MASS, "elements": list(GOLDEN_ELEMENTS),
+                                       "source": "reference src/noa/pms/dcs.hh via oracle/ref_dcs_wrapper.cc"}))
+    path = os.path.join(HERE, "elastic_golden.npz")
+    np.savez_compressed(path, **out)
+    print(path, os.path.getsize(path), "bytes", len(out), "arrays")
+
+
 if __name__ == "__main__":
     main()
+    elastic()

@@ -65,3 +65,33 @@ def test_drop_in_errors_are_c10_errors(muons_cuda):
         muons_cuda.vmap(0, 0, d[::2], d[::2].contiguous(), d[::2].contiguous())
     with pytest.raises(RuntimeError, match="invalid element"):
         muons_cuda.bremsstrahlung(d, d, 22.0, 1e-7, 0)
+
+
+def test_per_k_functions_through_the_drop_in(muons_cuda):
+    """recoil_integral, soft_scattering and the Coulomb chain through the
+    LibTorch layer, with the reference's argument order, against the oracle."""
+    K, _ = kinetic_recoil(3000, offset=123)
+    tk = torch.from_numpy(K).cuda()
+    out = torch.empty_like(tk)
+    muons_cuda.recoil_integral(1, 0, out, tk)
+    assert_fp64_parity(out.cpu().numpy(), oracle.recoil_integral(1, 0, K, 0.05, STANDARD_ROCK, MUON_MASS, 180),
+                       "recoil integral")
+    muons_cuda.soft_scattering(out, tk)
+    assert_fp64_parity(out.cpu().numpy(), oracle.soft_scattering(K, STANDARD_ROCK, MUON_MASS), "soft scattering")
+    n = K.size
+    f64 = dict(dtype=torch.float64, device="cuda")
+    fCM, screen, fspin, invlambda = (torch.zeros(n, 2, **f64), torch.zeros(n, 9, **f64), torch.zeros(n, **f64),
+                                     torch.zeros(n, **f64))
+    muons_cuda.coulomb_data(fCM, screen, fspin, invlambda, tk)
+    G = torch.zeros(n, 2, **f64)
+    muons_cuda.coulomb_transport(G, screen, fspin, torch.tensor(1.0, **f64))
+    mu0, lb_h = torch.zeros(n, **f64), torch.zeros(n, **f64)
+    muons_cuda.hard_scattering(mu0, lb_h, G.view(1, n, 2), fCM.view(1, n, 2), screen.view(1, n, 9),
+                               invlambda.view(1, n), fspin.view(1, n))
+    e = oracle.coulomb_data(K, STANDARD_ROCK, MUON_MASS)
+    eG = oracle.coulomb_transport(e[1], e[2], 1.0)
+    e_mu0, e_lb_h = oracle.hard_scattering(eG, e[0], e[1], e[3], e[2])
+    assert_fp64_parity(mu0.cpu().numpy(), e_mu0, "mu0")
+    assert_fp64_parity(lb_h.cpu().numpy(), e_lb_h, "lb_h")
+    with pytest.raises(RuntimeError):
+        muons_cuda.coulomb_transport(G, screen, fspin, torch.zeros(5, **f64))
