@@ -277,8 +277,10 @@ int noa_dcs_probe_fma(int fp64, void *out, int blocks, int iters, double *flops,
 
 /* Diagnostics (no counterpart in the reference): out[i] = f(x[i]) (or
  * f(x[i], y[i])) for one of the library's FP64 elementary functions --
- * fn 0 log, 1 exp, 2 reciprocal, 3 division x/y, 4 sqrt -- on device buffers,
- * so that their error can be measured against a reference libm. */
+ * fn 0 log, 1 exp, 2 reciprocal, 3 division x/y, 4 sqrt -- or of its
+ * integer-pipe conversions -- fn 5 (double)(float)x, 6 (double)(int)x for x
+ * in int range -- on device buffers, so that their error can be measured
+ * against a reference libm and the conversions checked against the casts. */
 int noa_dcs_lean64_eval(int fn, const double *x, const double *y, double *out, int64_t n, void *stream);
 
 #ifdef __cplusplus

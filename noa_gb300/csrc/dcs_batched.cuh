@@ -157,24 +157,6 @@ __device__ __forceinline__ void batch_step(double *wK, double *wQ, int64_t *wI, 
     }
 }
 
-template <int PROC, int THREADS>
-__device__ __forceinline__ void batch_drain_redo(double *rK, double *rQ, int64_t *rI, int *rn, double *out,
-                                                 const noa_dcs_consts &c, bool all) {
-    __syncthreads();
-    while (*rn >= (all ? 1 : THREADS)) {
-        const int n = *rn;
-        const int take = n < THREADS ? n : THREADS;
-        if ((int)threadIdx.x < take) {
-            const int e = n - take + threadIdx.x;
-            out[rI[e]] = batch_eval64<PROC>(rK[e], rQ[e], c);
-        }
-        __syncthreads();
-        if (threadIdx.x == 0)
-            *rn = n - take;
-        __syncthreads();
-    }
-}
-
 template <int PROC, int PREC, int THREADS>
 __global__ void __launch_bounds__(THREADS) dcs_batched_kernel(const __grid_constant__ BatchParams p) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -211,15 +193,42 @@ __global__ void __launch_bounds__(THREADS) dcs_batched_kernel(const __grid_const
             while (seg > 0 && tile < p.tile_begin[seg])
                 seg--;
         }
-        if (cur >= 0 && (done || seg != cur)) {
-            // element changes: finish the queued pairs of the current one
+        if (cur >= 0) {
+            // Drain the queues of the current element: full batches, or
+            // everything when the element changes or the work is done.  One
+            // call site each for the step and the redo, so that a pair's result
+            // does not depend on where it sits in the queue (nvcc may contract
+            // differently in separately inlined copies).
+            const bool flush = done || seg != cur;
             const noa_dcs_consts &cc = p.consts[cur];
-            batch_step<PROC, PREC>(wK, wQ, wI, rK, rQ, rI, &rn, threadIdx.x, (int)threadIdx.x < qn, p.out, cc,
-                                   p.tol);
-            qn = 0;
-            if (PREC != NOA_DCS_FP64)
-                batch_drain_redo<PROC, THREADS>(rK, rQ, rI, &rn, p.out, cc, true);
-            __syncthreads();
+            for (;;) {
+                bool did = false;
+                if (qn >= THREADS || (flush && qn > 0)) {
+                    const int take = qn < THREADS ? qn : THREADS;
+                    batch_step<PROC, PREC>(wK, wQ, wI, rK, rQ, rI, &rn, qn - take + threadIdx.x,
+                                           (int)threadIdx.x < take, p.out, cc, p.tol);
+                    qn -= take;
+                    did = true;
+                }
+                __syncthreads();
+                if (PREC != NOA_DCS_FP64) {
+                    const int r = rn;
+                    if (r >= THREADS || (flush && qn == 0 && r > 0)) {
+                        const int take = r < THREADS ? r : THREADS;
+                        if ((int)threadIdx.x < take) {
+                            const int e = r - take + threadIdx.x;
+                            p.out[rI[e]] = batch_eval64<PROC>(rK[e], rQ[e], cc);
+                        }
+                        __syncthreads();
+                        if (threadIdx.x == 0)
+                            rn = r - take;
+                        __syncthreads();
+                        did = true;
+                    }
+                }
+                if (!did)
+                    break;
+            }
         }
         if (done)
             break;
@@ -256,14 +265,6 @@ __global__ void __launch_bounds__(THREADS) dcs_batched_kernel(const __grid_const
         }
         __syncthreads();
         qn += tile_open;
-        while (qn >= THREADS) {
-            batch_step<PROC, PREC>(wK, wQ, wI, rK, rQ, rI, &rn, qn - THREADS + threadIdx.x, true, p.out, c, p.tol);
-            qn -= THREADS;
-            if (PREC != NOA_DCS_FP64)
-                batch_drain_redo<PROC, THREADS>(rK, rQ, rI, &rn, p.out, c, false);
-            else
-                __syncthreads();
-        }
     }
 }
 

@@ -14,6 +14,7 @@
 #pragma once
 
 #include "dcs_consts.h"
+#include "fpconv.cuh"
 
 #include <math.h>
 

@@ -142,22 +142,6 @@ __device__ __forceinline__ void fp32_step(Queues &s, int e, bool valid, double *
 }
 
 template <int PROC>
-__device__ __forceinline__ void drain_redo(Queues &s, double *out, const noa_dcs_consts &c, bool all) {
-    __syncthreads();
-    while (s.rn >= (all ? 1 : F_THREADS)) {
-        const int take = s.rn < F_THREADS ? s.rn : F_THREADS;
-        if ((int)threadIdx.x < take) {
-            const int e = s.rn - take + threadIdx.x;
-            out[s.rI[e]] = eval64<PROC>(s.rK[e], s.rQ[e], c);
-        }
-        __syncthreads();
-        if (threadIdx.x == 0)
-            s.rn -= take;
-        __syncthreads();
-    }
-}
-
-template <int PROC>
 __global__ void __launch_bounds__(F_THREADS) dcs_fp32c_kernel(const double *__restrict__ K,
                                                               const double *__restrict__ q, double *out, int64_t n,
                                                               const noa_dcs_consts c, float tol) {
@@ -165,41 +149,68 @@ __global__ void __launch_bounds__(F_THREADS) dcs_fp32c_kernel(const double *__re
     if (threadIdx.x == 0)
         s.rn = 0;
     int qn = 0;
-    for (int64_t base = (int64_t)blockIdx.x * F_TILE; base < n; base += (int64_t)gridDim.x * F_TILE) {
-        double k[F_ITEMS], r[F_ITEMS];
-        unsigned open = 0;
+    int64_t base = (int64_t)blockIdx.x * F_TILE;
+    for (;;) {
+        const bool more = base < n;  // block-uniform
+        if (more) {
+            double k[F_ITEMS], r[F_ITEMS];
+            unsigned open = 0;
 #pragma unroll
-        for (int j = 0; j < F_ITEMS; j++) {
-            const int64_t i = base + j * F_THREADS + threadIdx.x;
-            if (i < n) {
-                k[j] = K[i];
-                r[j] = q[i];
-                if (open32<PROC>(k[j], r[j], c))
-                    open |= 1u << j;
-                else
-                    out[i] = 0.;
+            for (int j = 0; j < F_ITEMS; j++) {
+                const int64_t i = base + j * F_THREADS + threadIdx.x;
+                if (i < n) {
+                    k[j] = K[i];
+                    r[j] = q[i];
+                    if (open32<PROC>(k[j], r[j], c))
+                        open |= 1u << j;
+                    else
+                        out[i] = 0.;
+                }
             }
-        }
-        int pos = qn + scan_block(__popc(open), s.warp_tot, &s.tile_open);
+            int pos = qn + scan_block(__popc(open), s.warp_tot, &s.tile_open);
 #pragma unroll
-        for (int j = 0; j < F_ITEMS; j++) {
-            if (open & (1u << j)) {
-                s.wK[pos] = k[j];
-                s.wQ[pos] = r[j];
-                s.wI[pos] = base + j * F_THREADS + threadIdx.x;
-                pos++;
+            for (int j = 0; j < F_ITEMS; j++) {
+                if (open & (1u << j)) {
+                    s.wK[pos] = k[j];
+                    s.wQ[pos] = r[j];
+                    s.wI[pos] = base + j * F_THREADS + threadIdx.x;
+                    pos++;
+                }
             }
+            __syncthreads();
+            qn += s.tile_open;
+            base += (int64_t)gridDim.x * F_TILE;
         }
-        __syncthreads();
-        qn += s.tile_open;
-        while (qn >= F_THREADS) {
-            fp32_step<PROC>(s, qn - F_THREADS + threadIdx.x, true, out, c, tol);
-            qn -= F_THREADS;
-            drain_redo<PROC>(s, out, c, false);
+        // One call site each for the FP32 step and the FP64 redo (see the
+        // FP64 kernels): full batches while tiles remain, everything at the end.
+        for (;;) {
+            bool did = false;
+            if (qn >= F_THREADS || (!more && qn > 0)) {
+                const int take = qn < F_THREADS ? qn : F_THREADS;
+                fp32_step<PROC>(s, qn - take + threadIdx.x, (int)threadIdx.x < take, out, c, tol);
+                qn -= take;
+                did = true;
+            }
+            __syncthreads();
+            const int rn = s.rn;
+            if (rn >= F_THREADS || (!more && qn == 0 && rn > 0)) {
+                const int take = rn < F_THREADS ? rn : F_THREADS;
+                if ((int)threadIdx.x < take) {
+                    const int e = rn - take + threadIdx.x;
+                    out[s.rI[e]] = eval64<PROC>(s.rK[e], s.rQ[e], c);
+                }
+                __syncthreads();
+                if (threadIdx.x == 0)
+                    s.rn = rn - take;
+                __syncthreads();
+                did = true;
+            }
+            if (!did)
+                break;
         }
+        if (!more)
+            break;
     }
-    fp32_step<PROC>(s, threadIdx.x, (int)threadIdx.x < qn, out, c, tol);
-    drain_redo<PROC>(s, out, c, true);
 }
 
 static int sm_count() {

@@ -72,13 +72,13 @@ struct KSum {
         c += (fabsf(s) >= fabsf(v)) ? ((s - t) + v) : ((v - t) + s);
         s = t;
     }
-    NOA_HD double value() const { return (double)s + (double)c; }
+    NOA_HD double value() const { return fpconv::f64(s) + fpconv::f64(c); }
 };
 
 // exp(uh + ul) and -expm1(uh + ul) for a double argument split into floats.
 NOA_HD void f_exp_split(double u, float &e, float &em1) {
-    const float uh = (float)u;
-    const float ul = (float)(u - (double)uh);
+    const float uh = fpconv::f32(u);
+    const float ul = fpconv::f32(u - fpconv::f64(uh));
     const float eh = expf(uh);
     e = fmaf(eh, ul, eh);
     em1 = fmaf(eh, ul, expm1f(uh));
@@ -88,24 +88,24 @@ NOA_HD void f_exp_split(double u, float &e, float &em1) {
 NOA_HD double brems_fp32c(double K, double q, const noa_dcs_consts &c, float &est) {
     est = 0.f;
     const double E = K + c.mass;
-    const float Ef = (float)E, qf = (float)q;
+    const float Ef = fpconv::f32(E), qf = fpconv::f32(q);
     // q < qe_max (physics.hh:142): float decision, exact when close
-    const float qe = f_div(Ef, 1.f + (float)c.br_half_m2 * f_rcp((float)ME * Ef));
+    const float qe = f_div(Ef, 1.f + fpconv::f32(c.br_half_m2) * f_rcp((float)ME * Ef));
     bool below = qf < qe;
     if (fabsf(qf - qe) <= 1e-5f * qe)
         below = brems_below_qe(E, q, c);
-    const float Emq = (float)(E - q);
+    const float Emq = fpconv::f32(E - q);
     const float sqrte = 1.648721271f;
     // delta = 0.5 m^2 nu / (E (1 - nu)) = 0.5 m^2 q / (E (E - q))
-    const float delta = (float)c.br_half_m2 * qf * f_rcp(Ef * Emq);
-    const float BZn = (float)c.br_BZ_n, Dn = (float)c.br_D_n, BZe = (float)c.br_BZ_e;
-    const float Phi_n = logf((BZn * ((float)c.mass + delta * (float)c.br_Dn_sqrte_m2)) *
+    const float delta = fpconv::f32(c.br_half_m2) * qf * f_rcp(Ef * Emq);
+    const float BZn = fpconv::f32(c.br_BZ_n), Dn = fpconv::f32(c.br_D_n), BZe = fpconv::f32(c.br_BZ_e);
+    const float Phi_n = logf((BZn * (fpconv::f32(c.mass) + delta * fpconv::f32(c.br_Dn_sqrte_m2))) *
                              f_rcp(Dn * ((float)ME + delta * sqrte * BZn)));
     float Phi_e = 0.f;
     if (below)
-        Phi_e = logf((float)c.br_BZe_mass *
-                     f_rcp((1.f + delta * (float)c.br_phie_factor) * ((float)ME + delta * sqrte * BZe)));
-    const float Zf = (float)c.Zd;
+        Phi_e = logf(fpconv::f32(c.br_BZe_mass) *
+                     f_rcp((1.f + delta * fpconv::f32(c.br_phie_factor)) * ((float)ME + delta * sqrte * BZe)));
+    const float Zf = fpconv::f32(c.Zd);
     const float S = Zf * f_clamp0(Phi_n) + f_clamp0(Phi_e);
     // 4/3 (1/nu - 1) + nu = 4/3 (E - q)/q + q/E
     const float fac = 1.33333333f * Emq * f_rcp(qf) + qf * f_rcp(Ef);
@@ -114,7 +114,7 @@ NOA_HD double brems_fp32c(double K, double q, const noa_dcs_consts &c, float &es
     if (!(S > 0.f) || !(Phi_n > 16.f * U32 || Phi_n < -16.f * U32) ||
         (below && !(Phi_e > 16.f * U32 || Phi_e < -16.f * U32)))
         est = INFINITY;
-    const double dcs = (double)(S * fac) * (c.br_dcs_factor * c.scale_A);
+    const double dcs = fpconv::f64(S * fac) * (c.br_dcs_factor * c.scale_A);
     return (dcs < 0.) ? 0. : dcs;
 }
 
@@ -146,12 +146,12 @@ NOA_HD double pprod_fp32c(double K, double q, const noa_dcs_consts &c, float &es
     // beta = 0.5 nu^2 / (1 - nu) = 0.5 q^2 / (E (E - q))
     const double beta_d = 0.5 * q * q * d_rcp(E * Emq);
     const double tmin_d = d_log(argmin);
-    const float tmin = (float)tmin_d;
-    const float beta = (float)beta_d;
-    const float xi_factor = (float)(c.pp_half_r2 * beta_d);
-    const float qf = (float)q;
-    const float AZ13 = (float)c.pp_AZ13, cL = (float)c.pp_cL, cLe = (float)c.pp_cLe;
-    const float rAZ13 = (float)c.pp_r_AZ13, Z13_15 = (float)c.pp_15_Z13, inv_r2 = (float)c.pp_inv_r2;
+    const float tmin = fpconv::f32(tmin_d);
+    const float beta = fpconv::f32(beta_d);
+    const float xi_factor = fpconv::f32(c.pp_half_r2 * beta_d);
+    const float qf = fpconv::f32(q);
+    const float AZ13 = fpconv::f32(c.pp_AZ13), cL = fpconv::f32(c.pp_cL), cLe = fpconv::f32(c.pp_cLe);
+    const float rAZ13 = fpconv::f32(c.pp_r_AZ13), Z13_15 = fpconv::f32(c.pp_15_Z13), inv_r2 = fpconv::f32(c.pp_inv_r2);
     const float b2 = 2.f * beta, b15 = 1.5f * beta, b3 = 3.f * beta, b4 = 4.f * beta;
     const float GL8W[8] = {0.05061427f, 0.11119052f, 0.15685332f, 0.18134189f,
                            0.18134189f, 0.15685332f, 0.11119052f, 0.05061427f};
@@ -240,17 +240,17 @@ NOA_HD double pprod_fp32c(double K, double q, const noa_dcs_consts &c, float &es
     const double gamma = 1. + K * c.inv_mass;
     float zeta = 0.f;
     if (!(gamma <= 35.)) {
-        const float gf = (float)gamma, Z13 = (float)c.pp_Z13;
-        zeta = 0.073f * logf(gf * f_rcp(1.f + (float)c.pp_gamma1 * gf * Z13 * Z13)) - 0.26f;
+        const float gf = fpconv::f32(gamma), Z13 = fpconv::f32(c.pp_Z13);
+        zeta = 0.073f * logf(gf * f_rcp(1.f + fpconv::f32(c.pp_gamma1) * gf * Z13 * Z13)) - 0.26f;
         if (zeta <= 0.f)
             zeta = 0.f;
         else
-            zeta = f_div(zeta, 0.058f * logf(gf * f_rcp(1.f + (float)c.pp_gamma2 * gf * Z13)) - 0.14f);
-        edge |= fabsf(gamma - 35.) < 1e-4;
+            zeta = f_div(zeta, 0.058f * logf(gf * f_rcp(1.f + fpconv::f32(c.pp_gamma2) * gf * Z13)) - 0.14f);
+        edge |= fabsf(gf - 35.f) < 1e-4f;
     }
     const double Id = I.value();
-    est = edge ? INFINITY : 1.3f * err * f_rcp((float)fabs(Id));  // calibrated: max error <= est
-    const double dcs = c.pp_cZ * (c.Zd + (double)zeta) * Emq * Id * d_rcp(q * E);
+    est = edge ? INFINITY : 1.3f * err * f_rcp(fpconv::f32(fabs(Id)));  // calibrated: max error <= est
+    const double dcs = c.pp_cZ * (c.Zd + fpconv::f64(zeta)) * Emq * Id * d_rcp(q * E);
     return (dcs < 0.) ? 0. : dcs * (mass + K) * c.scale_A;
 }
 
@@ -276,14 +276,14 @@ NOA_HD double photo_fp32c(double K, double q, const noa_dcs_consts &c, float &es
     const double dpQ2 = pQ2max - pQ2min;
     const double pQ2c = 0.5 * (pQ2max + pQ2min);
     const double inv_E = d_rcp(E);
-    const float omy = (float)((E - q) * inv_E);  // 1 - y, kinematic edge q -> E
-    const float y = (float)(q * inv_E);
+    const float omy = fpconv::f32((E - q) * inv_E);  // 1 - y, kinematic edge q -> E
+    const float y = fpconv::f32(q * inv_E);
     const double two_Mq_d = 2. * PH_M * q;
-    const float D = (float)(two_Mq_d - Q2max);  // 2Mq - Q2max = 2 M mpi + mpi^2 up to rounding
-    const float inv_2Mq = (float)d_rcp(two_Mq_d);
+    const float D = fpconv::f32(two_Mq_d - Q2max);  // 2Mq - Q2max = 2 M mpi + mpi^2 up to rounding
+    const float inv_2Mq = fpconv::f32(d_rcp(two_Mq_d));
     const float inv_Mq = 2.f * inv_2Mq;
-    const float Q2maxf = (float)Q2max;
-    const float half_dp = (float)(0.5 * dpQ2);
+    const float Q2maxf = fpconv::f32(Q2max);
+    const float half_dp = fpconv::f32(0.5 * dpQ2);
 
     const float m02 = 0.31985f, mP2 = 49.457f, mR2 = 0.15052f;
     const float cP1 = 0.28067f, cP2 = 0.22291f, cP3 = 2.1979f;
@@ -292,13 +292,13 @@ NOA_HD double photo_fp32c(double K, double q, const noa_dcs_consts &c, float &es
     const float cR1 = 0.80107f, cR2 = 0.97307f, cR3 = 3.4942f;
     const float aR1 = 0.58400f, aR2 = 0.37888f, aR3 = 2.6063f;
     const float bR1 = 0.01147f, bR2 = 3.7582f, bR3 = 0.49338f;
-    const float inv_P = (float)d_rcp(49.457 + two_Mq_d);
-    const float inv_R = (float)d_rcp(0.15052 + two_Mq_d);
+    const float inv_P = fpconv::f32(d_rcp(49.457 + two_Mq_d));
+    const float inv_R = fpconv::f32(d_rcp(0.15052 + two_Mq_d));
     const float inv_Q02 = 1.f / 0.52544f;
-    const float inv_LQ = (float)c.ph_inv_log_q02;
-    const float Af = (float)c.A, logA = (float)c.ph_logA, a_low = (float)c.ph_a_low;
-    const float two_m2 = (float)(2. * mass * mass);
-    const float invEE = (float)(inv_E * inv_E);
+    const float inv_LQ = fpconv::f32(c.ph_inv_log_q02);
+    const float Af = fpconv::f32(c.A), logA = fpconv::f32(c.ph_logA), a_low = fpconv::f32(c.ph_a_low);
+    const float two_m2 = fpconv::f32(2. * mass * mass);
+    const float invEE = fpconv::f32(inv_E * inv_E);
     const float yy = y * y;
     const float GL9X[9] = {0.0000000000000000f, -0.8360311073266358f, 0.8360311073266358f,
                            -0.9681602395076261f, 0.9681602395076261f, -0.3242534234038089f,
@@ -374,7 +374,7 @@ NOA_HD double photo_fp32c(double K, double q, const noa_dcs_consts &c, float &es
         err += GL9W[j] * (fabsf(g) * (eF2 + ea + 4.f * U32) + fabsf(F2A * Q2) * e_dds);
     }
     const double ds_f = S.value();
-    est = edge ? INFINITY : 0.6f * err * f_rcp((float)fabs(ds_f));  // calibrated: max error <= est
+    est = edge ? INFINITY : 0.6f * err * f_rcp(fpconv::f32(fabs(ds_f)));  // calibrated: max error <= est
     const double ds = ds_f * 2.603096E-35 * d_rcp(q);
     return (ds < 0.) ? 0. : 0.5 * ds * dpQ2 * (mass + K) * c.scale_A;
 }
@@ -398,12 +398,12 @@ NOA_HD double ion_fp32c(double K, double q, const noa_dcs_consts &c, float &est)
     const double cs = c.io_cZA * E * (0.5 * inv_P2 + inv_q * (E * E * inv_P2 * inv_q - d_rcp(Wmax)));
     float Delta = 0.f;
     if (K >= c.io_k_rad) {
-        const float L1 = log1pf((float)(q * (2. / ME)));
-        const float Ef = (float)E;
-        Delta = 1.16141E-03f * L1 * (logf(4.f * Ef * (float)(E - q) * (float)c.inv_m2) - L1);
+        const float L1 = log1pf(fpconv::f32(q * (2. / ME)));
+        const float Ef = fpconv::f32(E);
+        Delta = 1.16141E-03f * L1 * (logf(4.f * Ef * fpconv::f32(E - q) * fpconv::f32(c.inv_m2)) - L1);
     }
     est = fabsf(Delta) * 8.f * U32;  // the float part is Delta, relative to 1 + Delta
-    return cs * (1. + (double)Delta);
+    return cs * (1. + fpconv::f64(Delta));
 }
 
 } // namespace noa_dcs

@@ -18,6 +18,13 @@
  *    the last tile.  This is the warp-uniform regime grouping of the hot path;
  *    it needs no global scratch.
  *
+ * Each kernel calls the evaluation from exactly one place.  nvcc inlines
+ * every call site separately and may contract a * b + c into an FMA
+ * differently in each copy, so two call sites (a full-batch drain and a tail,
+ * or an unrolled item loop) could round the same pair differently depending
+ * on where it sits in the queue.  With one call site a pair's result depends
+ * on (K, q) only.
+ *
  * The reference launches one thread per pair on the legacy stream
  * (common.cuh:33-56) and recomputes three pow() per bremsstrahlung evaluation
  * (physics.hh:126-128); it has no GPU pair-production, photonuclear or
@@ -63,17 +70,10 @@ __global__ void __launch_bounds__(MAP_THREADS) dcs_fp64_map_kernel(const double 
                                                                    int64_t n, const noa_dcs_consts c) {
     const int64_t tile = (int64_t)MAP_THREADS * MAP_ITEMS;
     for (int64_t base = (int64_t)blockIdx.x * tile; base < n; base += (int64_t)gridDim.x * tile) {
-        double k[MAP_ITEMS], r[MAP_ITEMS];
-#pragma unroll
+#pragma unroll 1  // one inlined copy of the evaluation
         for (int j = 0; j < MAP_ITEMS; j++) {
             const int64_t i = base + j * MAP_THREADS + threadIdx.x;
-            k[j] = i < n ? K[i] : 1.;
-            r[j] = i < n ? q[i] : 1.;
-        }
-#pragma unroll
-        for (int j = 0; j < MAP_ITEMS; j++) {
-            const int64_t i = base + j * MAP_THREADS + threadIdx.x;
-            const double v = eval_fp64<PROC>(k[j], r[j], c);
+            const double v = eval_fp64<PROC>(i < n ? K[i] : 1., i < n ? q[i] : 1., c);
             if (i < n)
                 out[i] = v;
         }
@@ -112,7 +112,7 @@ __device__ __forceinline__ int block_exclusive_scan(int v, int *warp_tot, int *t
 }
 
 template <int PROC>
-__global__ void __launch_bounds__(CMP_THREADS) dcs_fp64_compact_kernel(const double *__restrict__ K,
+__global__ void __launch_bounds__(CMP_THREADS, PROC == NOA_DCS_PROC_PHOTO ? 4 : 2) dcs_fp64_compact_kernel(const double *__restrict__ K,
                                                                        const double *__restrict__ q, double *out,
                                                                        int64_t n, const noa_dcs_consts c) {
     __shared__ double qK[CMP_QCAP];
@@ -121,45 +121,51 @@ __global__ void __launch_bounds__(CMP_THREADS) dcs_fp64_compact_kernel(const dou
     __shared__ int warp_tot[CMP_THREADS / 32];
     __shared__ int tile_live;
     int qn = 0; // queue length, identical in every thread
-
-    for (int64_t base = (int64_t)blockIdx.x * CMP_TILE; base < n; base += (int64_t)gridDim.x * CMP_TILE) {
-        double k[CMP_ITEMS], r[CMP_ITEMS];
-        unsigned live = 0;
+    int64_t base = (int64_t)blockIdx.x * CMP_TILE;
+    for (;;) {
+        const bool more = base < n;  // block-uniform
+        if (more) {
+            double k[CMP_ITEMS], r[CMP_ITEMS];
+            unsigned live = 0;
 #pragma unroll
-        for (int j = 0; j < CMP_ITEMS; j++) {
-            const int64_t i = base + j * CMP_THREADS + threadIdx.x;
-            if (i < n) {
-                k[j] = K[i];
-                r[j] = q[i];
-                if (live_fp64<PROC>(k[j], r[j], c))
-                    live |= 1u << j;
-                else
-                    out[i] = 0.;
+            for (int j = 0; j < CMP_ITEMS; j++) {
+                const int64_t i = base + j * CMP_THREADS + threadIdx.x;
+                if (i < n) {
+                    k[j] = K[i];
+                    r[j] = q[i];
+                    if (live_fp64<PROC>(k[j], r[j], c))
+                        live |= 1u << j;
+                    else
+                        out[i] = 0.;
+                }
             }
-        }
-        const int mine = __popc(live);
-        int pos = qn + block_exclusive_scan(mine, warp_tot, &tile_live);
+            const int mine = __popc(live);
+            int pos = qn + block_exclusive_scan(mine, warp_tot, &tile_live);
 #pragma unroll
-        for (int j = 0; j < CMP_ITEMS; j++) {
-            if (live & (1u << j)) {
-                qK[pos] = k[j];
-                qQ[pos] = r[j];
-                qI[pos] = base + j * CMP_THREADS + threadIdx.x;
-                pos++;
+            for (int j = 0; j < CMP_ITEMS; j++) {
+                if (live & (1u << j)) {
+                    qK[pos] = k[j];
+                    qQ[pos] = r[j];
+                    qI[pos] = base + j * CMP_THREADS + threadIdx.x;
+                    pos++;
+                }
             }
+            __syncthreads();
+            qn += tile_live;
+            base += (int64_t)gridDim.x * CMP_TILE;
         }
-        __syncthreads();
-        qn += tile_live;
-        while (qn >= CMP_THREADS) {
-            const int e = qn - CMP_THREADS + threadIdx.x;
-            out[qI[e]] = eval_fp64<PROC>(qK[e], qQ[e], c);
-            qn -= CMP_THREADS;
+        // full batches while tiles remain, then the remainder: one call site
+        while (qn >= CMP_THREADS || (!more && qn > 0)) {
+            const int take = qn < CMP_THREADS ? qn : CMP_THREADS;
+            if ((int)threadIdx.x < take) {
+                const int e = qn - take + threadIdx.x;
+                out[qI[e]] = eval_fp64<PROC>(qK[e], qQ[e], c);
+            }
+            qn -= take;
             __syncthreads();
         }
-    }
-    if ((int)threadIdx.x < qn) {
-        const int e = threadIdx.x;
-        out[qI[e]] = eval_fp64<PROC>(qK[e], qQ[e], c);
+        if (!more)
+            break;
     }
 }
 

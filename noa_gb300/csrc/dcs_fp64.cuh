@@ -93,10 +93,10 @@ __device__ __forceinline__ bool pprod_live(double K, double q, const noa_dcs_con
         return false;
     // argmin in float (K - q formed in double: gamma - q/m = 1 + (K - q)/m);
     // the reference's IEEE value decides only within 1e-5 of a bound
-    const float im = (float)c.inv_mass;
-    const float x0 = (float)(4. * ME) * lean64::rcp_approx((float)q);
-    const float gamma = 1.f + (float)K * im;
-    const float x1 = 6.f * lean64::rcp_approx(gamma * (1.f + (float)(K - q) * im));
+    const float im = fpconv::f32(c.inv_mass);
+    const float x0 = (float)(4. * ME) * lean64::rcp_approx(fpconv::f32(q));
+    const float gamma = 1.f + fpconv::f32(K) * im;
+    const float x1 = 6.f * lean64::rcp_approx(gamma * (1.f + fpconv::f32(K - q) * im));
     const float a = (x0 + 2.f * (1.f - x0) * x1) * lean64::rcp_approx(1.f + (1.f - x1) * sqrtf(fmaxf(1.f - x0, 0.f)));
     if (!(fabsf(a - 1.f) > 1e-5f) || !(a > 1e-30f && a < 1e30f) || !(x0 < 0.9f)) {
         const double am = pprod_argmin_exact(K, q, c);
@@ -178,7 +178,33 @@ __device__ __forceinline__ double pprod_fp64(double K, double q, const noa_dcs_c
 }
 
 // ---------------------------------------------------------------- photonuclear
+// photo_window's open / closed decision (dcs.hh:357-381), float first: in
+// float every bound is decided with a relative margin of 1e-5 (1e-4 of the
+// terms for Q2max >= Q2min, whose float difference cancels near q_min; with
+// q_min = mpi (1 + mpi / 2M), Q2max = 2M (q - q_min) exactly in real
+// arithmetic), far above float rounding; pairs within a margin, and inputs
+// outside the float-safe range (zero, NaN, inf, huge), take the exact IEEE
+// check.  Only the closed / open answer is taken from float, never a value.
 __device__ __forceinline__ bool photo_live(double K, double q, const noa_dcs_consts &c) {
+    const float Kf = fpconv::f32(K), qf = fpconv::f32(q);
+    if (Kf >= 1e-30f && Kf <= 1e30f && qf >= 1e-30f && qf <= 1e30f) {
+        constexpr float lo = 0.99999f, hi = 1.00001f;
+        const float qmin = fpconv::f32(c.ph_q_min), cut = 2E-03f * Kf;
+        if (qf < lo || qf < cut * lo || qf > Kf * hi || qf < qmin * lo)
+            return false;  // q < 1, q < 2e-3 K, q >= E - m (= K to an ulp), q <= q_min
+        if (!(qf < hi || qf < cut * hi || qf > Kf * lo || qf < qmin * hi)) {
+            const float m = fpconv::f32(c.mass);
+            const float Ef = Kf + m, Emq = fpconv::f32(K + c.mass - q);  // q < K (1 - 1e-5): no cancellation
+            const float y = qf / Ef, omy = Emq / Ef;
+            const float Q2min = m * m * y * y / omy;
+            const float Q2max = (float)(2.0 * PH_M) * (qf - qmin);
+            const float margin = 1e-4f * ((float)(2.0 * PH_M) * qf + Q2min);
+            if (Q2max < Q2min - margin)
+                return false;
+            if (Q2max > Q2min + margin)
+                return true;
+        }
+    }
     double a, b;
     return photo_window(K, q, c, a, b);
 }

@@ -157,45 +157,50 @@ __global__ void __launch_bounds__(I_THREADS) recoil_integral_kernel(const Integr
             const double lb = log(K * p.xlow), ub = log(K);
             sK[threadIdx.x] = K;
             sLb[threadIdx.x] = lb;
-            sH[threadIdx.x] = x_div(ub - lb, (double)p.n_itv);
+            sH[threadIdx.x] = x_div(ub - lb, fpconv::f64i(p.n_itv));
         }
         __syncthreads();
         int qn = 0;
-        for (int base = 0; base < pairs; base += I_THREADS) {
-            const int slot = base + threadIdx.x;
-            bool open = false;
-            double q = 0.;
-            if (slot < pairs) {
-                const int kk = slot / p.nodes, i = slot - kk * p.nodes;
-                vals[slot] = 0.;
-                const double K = sK[kk];
-                if (k0 + kk < p.n && !(PROC == NOA_DCS_PROC_ION && K <= ion_thr)) {
-                    // node i of the composite rule, numerics.hh:84-86, in IEEE order
-                    const double t = x_add(sLb[kk], x_mul(sH[kk], (double)(i / 6) + kGL6X[i % 6]));
-                    q = lean_exp(t);
-                    open = i_open<PROC>(K, q, c);
+        for (int base = 0;; base += I_THREADS) {
+            const bool more = base < pairs;  // block-uniform
+            if (more) {
+                const int slot = base + threadIdx.x;
+                bool open = false;
+                double q = 0.;
+                if (slot < pairs) {
+                    const int kk = slot / p.nodes, i = slot - kk * p.nodes;
+                    vals[slot] = 0.;
+                    const double K = sK[kk];
+                    if (k0 + kk < p.n && !(PROC == NOA_DCS_PROC_ION && K <= ion_thr)) {
+                        // node i of the composite rule, numerics.hh:84-86, in IEEE order
+                        const double t = x_add(sLb[kk], x_mul(sH[kk], fpconv::f64i(i / 6) + kGL6X[i % 6]));
+                        q = lean_exp(t);
+                        open = i_open<PROC>(K, q, c);
+                    }
                 }
+                const int pos = qn + i_scan(open ? 1 : 0, warp_tot, &tile_open);
+                if (open) {
+                    qQ[pos] = q;
+                    qS[pos] = slot;
+                }
+                __syncthreads();
+                qn += tile_open;
             }
-            int pos = qn + i_scan(open ? 1 : 0, warp_tot, &tile_open);
-            if (open) {
-                qQ[pos] = q;
-                qS[pos] = slot;
-            }
-            __syncthreads();
-            qn += tile_open;
-            while (qn >= I_THREADS) {
-                const int e = qn - I_THREADS + threadIdx.x;
-                const int sl = qS[e], kk = sl / p.nodes;
-                vals[sl] = i_node_value<PROC>(sK[kk], qQ[e], sH[kk], sl - kk * p.nodes, p.moment, c);
-                qn -= I_THREADS;
+            // one call site of the evaluation (a pair's rounding must not
+            // depend on its queue position): full batches, then the rest
+            while (qn >= I_THREADS || (!more && qn > 0)) {
+                const int take = qn < I_THREADS ? qn : I_THREADS;
+                if ((int)threadIdx.x < take) {
+                    const int e = qn - take + threadIdx.x;
+                    const int sl = qS[e], kk = sl / p.nodes;
+                    vals[sl] = i_node_value<PROC>(sK[kk], qQ[e], sH[kk], sl - kk * p.nodes, p.moment, c);
+                }
+                qn -= take;
                 __syncthreads();
             }
+            if (!more)
+                break;
         }
-        if ((int)threadIdx.x < qn) {
-            const int sl = qS[threadIdx.x], kk = sl / p.nodes;
-            vals[sl] = i_node_value<PROC>(sK[kk], qQ[threadIdx.x], sH[kk], sl - kk * p.nodes, p.moment, c);
-        }
-        __syncthreads();
         // one thread per kinetic energy: node-ordered sum, as the reference
         if ((int)threadIdx.x < p.kpt) {
             const int64_t ki = k0 + threadIdx.x;
@@ -289,7 +294,7 @@ __device__ __forceinline__ double soft_ionisation(double K, const noa_dcs_consts
 
 // Node i of the rule for kinetic energy K: nu and q (numerics.hh:84-86, dcs.hh:910-911).
 __device__ __forceinline__ void soft_node(double K, int i, const SoftParams &p, double &nu, double &q) {
-    const double t = x_add(p.lb, x_mul(p.h, (double)(i / 6) + kGL6X[i % 6]));
+    const double t = x_add(p.lb, x_mul(p.h, fpconv::f64i(i / 6) + kGL6X[i % 6]));
     nu = x_mul(NOA_X_FRACTION, exp(t));
     q = x_mul(nu, K);
 }
@@ -310,46 +315,47 @@ __global__ void __launch_bounds__(I_THREADS) soft_scattering_kernel(const SoftPa
         }
         __syncthreads();
         int qn = 0;
-        for (int base = 0; base < S_PAIRS; base += I_THREADS) {
-            const int slot = base + threadIdx.x;
-            bool open = false;
-            if (slot < S_PAIRS) {
-                const int kk = slot / S_NODES, i = slot - kk * S_NODES;
-                vals[slot] = 0.;
-                if (k0 + kk < p.n) {
+        for (int base = 0;; base += I_THREADS) {
+            const bool more = base < S_PAIRS;  // block-uniform
+            if (more) {
+                const int slot = base + threadIdx.x;
+                bool open = false;
+                if (slot < S_PAIRS) {
+                    const int kk = slot / S_NODES, i = slot - kk * S_NODES;
+                    vals[slot] = 0.;
+                    if (k0 + kk < p.n) {
+                        const double K = sK[kk];
+                        double nu, q;
+                        soft_node(K, i, p, nu, q);
+                        open = photo_live(K, q, c);
+                        if (!open)  // photonuclear = 0: 0 * ratio * nu * h * w
+                            vals[slot] =
+                                x_mul(x_mul(x_mul(x_mul(0., soft_ratio(K, q, c.mass)), nu), p.h), kGL6W[i % 6]);
+                    }
+                }
+                const int pos = qn + i_scan(open ? 1 : 0, warp_tot, &tile_open);
+                if (open)
+                    qS[pos] = slot;
+                __syncthreads();
+                qn += tile_open;
+            }
+            // one call site of the evaluation, as in the recoil integrals
+            while (qn >= I_THREADS || (!more && qn > 0)) {
+                const int take = qn < I_THREADS ? qn : I_THREADS;
+                if ((int)threadIdx.x < take) {
+                    const int sl = qS[qn - take + threadIdx.x];
+                    const int kk = sl / S_NODES, i = sl - kk * S_NODES;
                     const double K = sK[kk];
                     double nu, q;
                     soft_node(K, i, p, nu, q);
-                    open = photo_live(K, q, c);
-                    if (!open)  // photonuclear = 0: 0 * ratio * nu * h * w
-                        vals[slot] = x_mul(x_mul(x_mul(x_mul(0., soft_ratio(K, q, c.mass)), nu), p.h), kGL6W[i % 6]);
+                    const double f = x_mul(x_mul(photo_fp64(K, q, c), soft_ratio(K, q, c.mass)), nu);
+                    vals[sl] = x_mul(x_mul(f, p.h), kGL6W[i % 6]);
                 }
-            }
-            const int pos = qn + i_scan(open ? 1 : 0, warp_tot, &tile_open);
-            if (open)
-                qS[pos] = slot;
-            __syncthreads();
-            qn += tile_open;
-            while (qn >= I_THREADS) {
-                const int sl = qS[qn - I_THREADS + threadIdx.x];
-                const int kk = sl / S_NODES, i = sl - kk * S_NODES;
-                const double K = sK[kk];
-                double nu, q;
-                soft_node(K, i, p, nu, q);
-                const double f = x_mul(x_mul(photo_fp64(K, q, c), soft_ratio(K, q, c.mass)), nu);
-                vals[sl] = x_mul(x_mul(f, p.h), kGL6W[i % 6]);
-                qn -= I_THREADS;
+                qn -= take;
                 __syncthreads();
             }
-        }
-        if ((int)threadIdx.x < qn) {
-            const int sl = qS[threadIdx.x];
-            const int kk = sl / S_NODES, i = sl - kk * S_NODES;
-            const double K = sK[kk];
-            double nu, q;
-            soft_node(K, i, p, nu, q);
-            const double f = x_mul(x_mul(photo_fp64(K, q, c), soft_ratio(K, q, c.mass)), nu);
-            vals[sl] = x_mul(x_mul(f, p.h), kGL6W[i % 6]);
+            if (!more)
+                break;
         }
         __syncthreads();
         if ((int)threadIdx.x < S_KPT) {

@@ -1,7 +1,8 @@
 /*
- * Diagnostics entry point: evaluates one lean64 function (lean64.cuh)
- * element-wise so that tests can bound its error against a host libm.  No
- * counterpart in the reference.
+ * Diagnostics entry point: evaluates one lean64 function (lean64.cuh) or one
+ * integer-pipe conversion (fpconv.cuh) element-wise so that tests can bound
+ * its error against a host libm, or check it bit for bit against the cast it
+ * replaces.  No counterpart in the reference.
  */
 #include "dcs_launch.h"
 #include "lean64.cuh"
@@ -18,7 +19,9 @@ __global__ void lean64_eval_kernel(int fn, const double *__restrict__ x, const d
         case 1: r = lean64::lean_exp(a); break;
         case 2: r = lean64::lean_rcp(a); break;
         case 3: r = lean64::lean_div(a, y[i]); break;
-        default: r = lean64::lean_sqrt(a); break;
+        case 4: r = lean64::lean_sqrt(a); break;
+        case 5: r = fpconv::f64(fpconv::f32(a)); break;      // (double)(float)a
+        default: r = fpconv::f64i(__double2int_rz(a)); break;  // (double)(int)a
         }
         out[i] = r;
     }
@@ -27,7 +30,7 @@ __global__ void lean64_eval_kernel(int fn, const double *__restrict__ x, const d
 } // namespace
 
 extern "C" int noa_dcs_lean64_eval(int fn, const double *x, const double *y, double *out, int64_t n, void *stream) {
-    if (fn < 0 || fn > 4 || n < 0 || (n > 0 && (!x || !out || (fn == 3 && !y))))
+    if (fn < 0 || fn > 6 || n < 0 || (n > 0 && (!x || !out || (fn == 3 && !y))))
         return NOA_DCS_ERROR_INVALID_VALUE;
     if (n == 0)
         return NOA_DCS_SUCCESS;

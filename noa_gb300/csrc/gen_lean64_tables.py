@@ -55,9 +55,10 @@ def main():
     out.append(f"#define LEAN64_INV_LN2N {float(EXP_N / ln2)!r}")
     out.append(f"#define LEAN64_LN2N_HI {float(hi)!r}")
     out.append(f"#define LEAN64_LN2N_LO {float(lo)!r}")
-    out.append("/* 1/m_t rounded to float (1 for the two bins touching 1). */")
-    out.append("static __device__ const float lean64_log_c[%d] = {" % len(c))
-    out.append(",\n".join("    %.9ef" % v for v in c) + "};")
+    out.append("/* 1/m_t rounded to float (1 for the two bins touching 1), stored as")
+    out.append("   double so that no float -> double conversion is needed. */")
+    out.append("static __device__ const double lean64_log_c[%d] = {" % len(c))
+    out.append(",\n".join("    %r" % v for v in c) + "};")
     out.append("/* -log(c_t) rounded to double. */")
     out.append("static __device__ const double lean64_log_l[%d] = {" % len(L))
     out.append(",\n".join("    %s" % repr(v) for v in L) + "};")

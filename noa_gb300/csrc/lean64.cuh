@@ -29,9 +29,15 @@
  * Arguments outside the fast range (zero, negative, subnormal, |x| > 700
  * for exp, values outside float range for rcp/sqrt, inf, NaN) take CUDA's
  * IEEE function, so special values behave exactly as in IEEE arithmetic.
+ *
+ * The counts above are FP64-pipe instructions: the double <-> float and
+ * int -> double conversions between the FP64 and FP32 parts go through the
+ * integer pipe (fpconv.cuh), because the hardware conversions would occupy
+ * the FP64 pipe too.
  */
 #pragma once
 
+#include "fpconv.cuh"
 #include "lean64_tables.h"
 
 #include <cuda_runtime.h>
@@ -66,30 +72,30 @@ __device__ __forceinline__ double lean_log(double x) {
     const int shift = t >= LEAN64_LOG_SPLIT ? 1 : 0;
     const int e = (hi >> 20) - 1023 + shift;
     const double m = __longlong_as_double((b & 0x000FFFFFFFFFFFFFLL) | ((long long)(1023 - shift) << 52));
-    const double c = (double)__ldg(&lean64_log_c[t]);
+    const double c = __ldg(&lean64_log_c[t]);
     const double L = __ldg(&lean64_log_l[t]);
     const double r = fma(m, c, -1.0);
-    const float rf = (float)r;
+    const float rf = fpconv::f32(r);
     const float t5 = fmaf(rf, fmaf(rf, 1.f / 7.f, -1.f / 6.f), 1.f / 5.f);
     const double r2 = r * r;
-    double p = fma(r, (double)t5, -0.25);
+    double p = fma(r, fpconv::f64(t5), -0.25);
     p = fma(r, p, 1.0 / 3.0);
     p = fma(r, p, -0.5);
     p = fma(r2, p, r);
-    return fma((double)e, LEAN64_LN2, L) + p;
+    return fma(fpconv::f64i(e), LEAN64_LN2, L) + p;
 }
 
 __device__ __forceinline__ double lean_exp(double x) {
     if ((__double_as_longlong(x) & 0x7FFFFFFFFFFFFFFFLL) >= 0x4085E00000000000LL) // |x| >= 700, inf, NaN
         return exp(x);
-    const int k = __float2int_rn((float)x * (float)LEAN64_INV_LN2N);
-    const double kd = (double)k;
+    const int k = __float2int_rn(fpconv::f32(x) * (float)LEAN64_INV_LN2N);
+    const double kd = fpconv::f64i(k);
     double r = fma(-kd, LEAN64_LN2N_HI, x);
     r = fma(-kd, LEAN64_LN2N_LO, r);
-    const float rf = (float)r;
+    const float rf = fpconv::f32(r);
     const float t4 = fmaf(rf, 1.f / 120.f, 1.f / 24.f);
     const double r2 = r * r;
-    double p = fma(r, (double)t4, 1.0 / 6.0);
+    double p = fma(r, fpconv::f64(t4), 1.0 / 6.0);
     p = fma(r, p, 0.5);
     p = fma(r2, p, r);
     const double tj = __ldg(&lean64_exp_t[k & (LEAN64_EXP_N - 1)]);
@@ -99,11 +105,11 @@ __device__ __forceinline__ double lean_exp(double x) {
 }
 
 __device__ __forceinline__ double lean_rcp(double b) {
-    const float bf = (float)b;
+    const float bf = fpconv::f32(b);
     const float af = fabsf(bf);
     if (!(af >= 2e-38f && af <= 8e37f))  // 1/b must be a normal float too (the MUFU result is flushed)
         return 1.0 / b;
-    const double y = (double)rcp_approx(bf);
+    const double y = fpconv::f64(rcp_approx(bf));
     double e = fma(-b, y, 1.0);
     e = fma(e, e, e);
     return fma(y, e, y);
@@ -112,10 +118,10 @@ __device__ __forceinline__ double lean_rcp(double b) {
 __device__ __forceinline__ double lean_div(double a, double b) { return a * lean_rcp(b); }
 
 __device__ __forceinline__ double lean_sqrt(double x) {
-    const float xf = (float)x;
+    const float xf = fpconv::f32(x);
     if (!(xf >= 2e-38f && xf <= 1e38f))
         return sqrt(x);
-    const double y = (double)rsqrt_approx(xf);
+    const double y = fpconv::f64(rsqrt_approx(xf));
     const double h = 0.5 * y;
     double s = x * y;
     double r = fma(-s, s, x);

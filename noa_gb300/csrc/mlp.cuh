@@ -105,9 +105,9 @@ __device__ __forceinline__ bool baseline(double K, double q, const noa_dcs_const
 // rounding); the exact checks decide everything else.
 template <int PROC>
 __device__ __forceinline__ bool surely_closed(double K, double q, const noa_dcs_consts &c) {
-    const float Kf = (float)K, qf = (float)q;
+    const float Kf = fpconv::f32(K), qf = fpconv::f32(q);
     if (PROC == NOA_DCS_PAIR_PRODUCTION)
-        return qf < (float)(4. * noa_dcs::ME) * 0.99999f || qf > (Kf + (float)c.pp_kmax_shift) * 1.00001f;
+        return qf < (float)(4. * noa_dcs::ME) * 0.99999f || qf > (Kf + fpconv::f32(c.pp_kmax_shift)) * 1.00001f;
     return qf < 0.99999f || qf < 2E-03f * Kf * 0.99999f;
 }
 
@@ -118,20 +118,20 @@ __device__ __forceinline__ bool baseline_fast(double K, double q, const noa_dcs_
         return false;
     const double mass = c.mass;
     const double E = K + mass;
-    const float Ef = (float)E, qf = (float)q, Emq = (float)(E - q);
+    const float Ef = fpconv::f32(E), qf = fpconv::f32(q), Emq = fpconv::f32(E - q);
     if (PROC == NOA_DCS_PAIR_PRODUCTION) {
         if (!pprod_live(K, q, c))
             return false;
         // argmin in float (as pprod_live), its log, and the prefactor
-        const float im = (float)c.inv_mass;
+        const float im = fpconv::f32(c.inv_mass);
         const float x0 = (float)(4. * ME) / qf;
-        const float gamma = 1.f + (float)K * im;
-        const float x1 = 6.f / (gamma * (1.f + (float)(K - q) * im));
+        const float gamma = 1.f + fpconv::f32(K) * im;
+        const float x1 = 6.f / (gamma * (1.f + fpconv::f32(K - q) * im));
         const float a = (x0 + 2.f * (1.f - x0) * x1) / (1.f + (1.f - x1) * sqrtf(fmaxf(1.f - x0, 0.f)));
         // near argmin -> 1, -log(argmin) needs argmin's FP64 value
-        const float tmin = (a > 0.99f || !(x0 < 0.9f)) ? (float)d_log(pprod_argmin_exact(K, q, c)) : logf(a);
-        base = logf((float)(c.pp_cZ * c.Zd * c.scale_A)) + logf(Emq) - logf(qf) - logf(Ef) +
-               logf((float)(mass + K)) + logf(-tmin);
+        const float tmin = (a > 0.99f || !(x0 < 0.9f)) ? fpconv::f32(d_log(pprod_argmin_exact(K, q, c))) : logf(a);
+        base = logf(fpconv::f32(c.pp_cZ * c.Zd * c.scale_A)) + logf(Emq) - logf(qf) - logf(Ef) +
+               logf(fpconv::f32(mass + K)) + logf(-tmin);
         return true;
     } else {
         if ((q < 1.) || (q < 2E-03 * K))
@@ -139,8 +139,8 @@ __device__ __forceinline__ bool baseline_fast(double K, double q, const noa_dcs_
         if ((q >= (E - mass)) || (q <= c.ph_q_min))
             return false;
         const float y = qf / Ef, omy = Emq / Ef;
-        const float Q2min = (float)(mass * mass) * y * y / omy;
-        const float Q2max = (float)(2.0 * PH_M) * (float)(q - PH_MPI) - (float)(PH_MPI * PH_MPI);
+        const float Q2min = fpconv::f32(mass * mass) * y * y / omy;
+        const float Q2max = (float)(2.0 * PH_M) * fpconv::f32(q - PH_MPI) - (float)(PH_MPI * PH_MPI);
         if (fabsf(Q2max - Q2min) <= 1e-4f * fmaxf(fabsf(Q2max), fabsf(Q2min)) || !(Q2min > 0.f)) {
             double a, b;
             if (!photo_window(K, q, c, a, b))
@@ -148,8 +148,8 @@ __device__ __forceinline__ bool baseline_fast(double K, double q, const noa_dcs_
         } else if (Q2max < Q2min) {
             return false;
         }
-        base = logf((float)(2.603096E-35 * c.scale_A)) - logf(qf) + logf(omy + 0.5f * y * y) +
-               logf(1.f / Q2min - 1.f / Q2max) + logf((float)(mass + K));
+        base = logf(fpconv::f32(2.603096E-35 * c.scale_A)) - logf(qf) + logf(omy + 0.5f * y * y) +
+               logf(1.f / Q2min - 1.f / Q2max) + logf(fpconv::f32(mass + K));
         return true;
     }
 }

@@ -101,7 +101,7 @@ __global__ void __launch_bounds__(256) classify_kernel(const __grid_constant__ I
             if (!baseline_fast<PROC>(K, q, c, bf)) {
                 p.out[i] = 0.;
             } else {
-                const float lk = logf((float)K), ln = logf((float)q / (float)(K + c.mass));
+                const float lk = logf(fpconv::f32(K)), ln = logf(fpconv::f32(q) / fpconv::f32(K + c.mass));
                 const float fk = floorf((lk - p.logk_lo) / p.logk_span * 64.f);
                 const float fn = floorf((ln - p.lognu_lo) / p.lognu_span * 64.f);
                 bool trusted = false;
@@ -421,7 +421,7 @@ __global__ void __launch_bounds__(NT, 1) network_kernel(const __grid_constant__ 
         if (quarter == 0 && valid) {
             const float yy = y + spart[0][row] + spart[1][row] + spart[2][row] + bo;
             const float r = p.norm.out_shift + yy / p.norm.out_scale;
-            p.out[p.net_idx[e]] = (double)expf(p.net_base[e] + r);
+            p.out[p.net_idx[e]] = fpconv::f64(expf(p.net_base[e] + r));
         }
     }
     if (s_abort && tid == 0)

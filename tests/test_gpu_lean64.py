@@ -74,3 +74,35 @@ def test_reciprocal_division_sqrt(cuda_device):
             got = run(fn, special)
             assert np.array_equal(np.isnan(got), np.isnan(ref))
             assert np.array_equal(got[~np.isnan(ref)], ref[~np.isnan(ref)])
+
+
+def _bits(a):
+    return np.asarray(a, dtype=np.float64).view(np.uint64)
+
+
+def test_integer_pipe_float_conversion_is_the_cast(cuda_device):
+    """fpconv::f32 / f64 (integer-pipe conversions used on every hot path)
+    give exactly (double)(float)x: round to nearest even, ties, float
+    subnormals, overflow to infinity, signed zeros, NaN."""
+    rng = np.random.default_rng(7)
+    raw = rng.integers(0, 1 << 63, 400_000, dtype=np.uint64).view(np.float64)
+    wide = rng.standard_normal(200_000) * 10.0 ** rng.uniform(-50, 45, 200_000)
+    f = (rng.standard_normal(50_000) * 10.0 ** rng.uniform(-44, 38, 50_000)).astype(np.float32).astype(np.float64)
+    fb = f.view(np.uint64)
+    ties = np.concatenate([fb + (1 << 28), fb - (1 << 28), fb + (1 << 28) + 1]).view(np.float64)
+    special = np.array([0.0, -0.0, np.inf, -np.inf, np.nan, 1e-45, 7e-46, 1.4e-45, 3.4028235e38, 3.4028236e38,
+                        -3.5e38, 1.1754943e-38, 1.1754942e-38, 5.877472e-39, 1e-320, 1e300])
+    x = np.concatenate([raw, wide, ties, special])
+    got = run(5, x)
+    with np.errstate(over="ignore", invalid="ignore"):
+        exp = x.astype(np.float32).astype(np.float64)
+    nan = np.isnan(exp)
+    assert np.array_equal(np.isnan(got), nan)
+    assert np.array_equal(_bits(got[~nan]), _bits(exp[~nan]))
+
+
+def test_integer_pipe_int_conversion_is_the_cast(cuda_device):
+    rng = np.random.default_rng(8)
+    i = np.concatenate([rng.integers(-(1 << 31), 1 << 31, 200_000), [0, 1, -1, 2**31 - 1, -2**31, 1023, -1074]])
+    x = i.astype(np.float64)
+    assert np.array_equal(_bits(run(6, x)), _bits(x))
