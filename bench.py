@@ -84,20 +84,24 @@ def reduce_max(value, world, device=None):
 
 
 # ---------------------------------------------------------------- CPU side
-def cpu_reference_rate(n_sample, reps=3, offset=0):
-    """Evaluations/s of the oracle (reference algorithm) with every host
-    thread, on the first n_sample pairs of the workload, all four processes."""
+def cpu_reference_rate(n_sample, reps=5, offset=0, threads=0):
+    """Evaluations/s of the oracle (reference algorithm) on the first
+    n_sample pairs of the workload, all four processes, median of reps runs
+    after one warm-up; threads 0 = every host thread (dcs::pvmap), 1 = the
+    serial loop (dcs::vmap)."""
     import oracle
     from noa_gb300.elements import MUON_MASS, STANDARD_ROCK
     from noa_gb300.workload import kinetic_recoil
     K, q = kinetic_recoil(n_sample, offset=offset)
+    for p in range(4):
+        oracle.dcs(p, K, q, STANDARD_ROCK, MUON_MASS, threads=threads)
     per = {}
     total_t = []
     for _ in range(reps):
         t_all = 0.0
         for p, name in enumerate(PROCESSES):
             t0 = time.perf_counter()
-            oracle.dcs(p, K, q, STANDARD_ROCK, MUON_MASS, threads=0)
+            oracle.dcs(p, K, q, STANDARD_ROCK, MUON_MASS, threads=threads)
             dt = time.perf_counter() - t0
             per.setdefault(name, []).append(dt)
             t_all += dt
@@ -107,7 +111,7 @@ def cpu_reference_rate(n_sample, reps=3, offset=0):
         "value": 4 * n_sample / t,
         "seconds_per_sample": t,
         "per_process": {k: n_sample / statistics.median(v) for k, v in per.items()},
-        "cores": oracle.lib().oracle_max_threads(),
+        "cores": oracle.lib().oracle_max_threads() if threads == 0 else threads,
     }
 
 
@@ -415,7 +419,7 @@ def time_surrogate(torch, args):
     GPU (plain-kernel data, tensor-core forward / backward, Adam; moderate
     recipe), then evaluated on `surrogate_queries` seeded pairs over the 10
     elements: the network answers the pairs of trusted cells (held-out error
-    <= 5e-4), the FP32C kernel the rest.  Compared with the plain FP64 kernel
+    <= 3.5e-4), the FP32C kernel the rest.  Compared with the plain FP64 kernel
     and the FP32C kernel (batched engine, one launch) on the same pairs; error
     against the plain FP64 output."""
     from noa_gb300.batched import BatchPlan, batch_inputs
@@ -614,9 +618,13 @@ def run_ours(args):
         line["surrogate"] = time_surrogate(torch, args)
     if not args.no_cpu_baseline and world == 1:
         cb = cpu_reference_rate(min(n, 1_000_000))
+        c1 = cpu_reference_rate(min(n, 100_000), reps=3, threads=1)
         line["cpu_baseline"] = {"value": cb["value"], "unit": "evals/s", "cores": cb["cores"], "kind": "port",
-                                "sample": "first 1e6 pairs of the workload, all four processes, median of 3",
-                                "per_process": cb["per_process"]}
+                                "sample": "first 1e6 pairs of the workload, all four processes, median of 5 "
+                                          "after a warm-up",
+                                "per_process": cb["per_process"],
+                                "single_thread": {"value": c1["value"], "per_process": c1["per_process"],
+                                                  "sample": "first 1e5 pairs, median of 3"}}
     print(json.dumps(line), flush=True)
     if world > 1:
         tdist.destroy_process_group()

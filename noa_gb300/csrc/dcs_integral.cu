@@ -268,6 +268,32 @@ __device__ __forceinline__ double soft_ratio(double K, double q, double mass) {
                  x_mul(x_mul(x_sub(x_mul(I0, tmax), I1), K), x_add(K, x_mul(2., mass))));
 }
 
+// The same weight with the lean functions, for closed photonuclear nodes:
+// there the reference adds 0 * ratio * nu, which is 0 (of either sign, which
+// the node sum cannot tell apart) unless the ratio is not finite.  Only its
+// finiteness is used.
+__device__ __forceinline__ bool soft_ratio_finite(double K, double q, double mass) {
+    const double E = K + mass;
+    const double m02 = 0.4;
+    const double q2 = x_mul(q, q);
+    const double tmax = 1.876544 * q;
+    const double tmin = q2 * mass * mass * d_rcp(E * (E - q));
+    // the weight's poles (q^2 = m02) are decided in IEEE arithmetic as in the reference
+    const double b1 = d_rcp(x_sub(1., x_div(q2, m02)));
+    const double c1 = d_rcp(x_sub(1., x_div(m02, q2)));
+    double L1 = b1 * d_log((q2 + tmax) * d_rcp(q2 + tmin));
+    double L2 = c1 * d_log((m02 + tmax) * d_rcp(m02 + tmin));
+    const double I0 = d_log(tmax * d_rcp(tmin)) - L1 - L2;
+    L1 *= q2;
+    L2 *= m02;
+    const double I1 = L1 + L2;
+    L1 *= q2;
+    L2 *= m02;
+    const double I2 = (tmax - tmin) * (b1 * q2 + c1 * m02) - L1 - L2;
+    const double r = (I1 * tmax - I2) * d_rcp((I0 * tmax - I1) * K * (K + 2. * mass));
+    return isfinite(r);
+}
+
 // dcs.hh:874-899 in the reference's operation order.
 __device__ __forceinline__ double soft_ionisation(double K, const noa_dcs_consts &c) {
     const double mass = c.mass;
@@ -328,9 +354,8 @@ __global__ void __launch_bounds__(I_THREADS) soft_scattering_kernel(const SoftPa
                         double nu, q;
                         soft_node(K, i, p, nu, q);
                         open = photo_live(K, q, c);
-                        if (!open)  // photonuclear = 0: 0 * ratio * nu * h * w
-                            vals[slot] =
-                                x_mul(x_mul(x_mul(x_mul(0., soft_ratio(K, q, c.mass)), nu), p.h), kGL6W[i % 6]);
+                        if (!open && !soft_ratio_finite(K, q, c.mass))  // photonuclear = 0: 0 * ratio * nu
+                            vals[slot] = __longlong_as_double(0x7FF8000000000000LL);   // NaN, as 0 * inf
                     }
                 }
                 const int pos = qn + i_scan(open ? 1 : 0, warp_tot, &tile_open);

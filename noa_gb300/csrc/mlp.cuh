@@ -134,9 +134,7 @@ __device__ __forceinline__ bool baseline_fast(double K, double q, const noa_dcs_
                logf(fpconv::f32(mass + K)) + logf(-tmin);
         return true;
     } else {
-        if ((q < 1.) || (q < 2E-03 * K))
-            return false;
-        if ((q >= (E - mass)) || (q <= c.ph_q_min))
+        if (!photo_live(K, q, c))  // float first, exact near the bounds
             return false;
         const float y = qf / Ef, omy = Emq / Ef;
         const float Q2min = fpconv::f32(mass * mass) * y * y / omy;
