@@ -246,7 +246,10 @@ const char *noa_dcs_mlp_last_error(void);
  * `tolerance`).  Closed pairs get 0.  stats (pinned or host memory, optional)
  * receives {network pairs, fallback pairs, status} when the stream reaches
  * it; status NOA_DCS_ERROR_TIMEOUT reports an expired tensor-core wait.
- * Allocates its pair lists on first use and when n grows. */
+ * Allocates its pair lists on first use and when n grows.  The lists are one
+ * per process: calls whose work overlaps on the GPU (other streams, other
+ * host threads) must be ordered by the caller.  K, q, result and trust must be
+ * device memory of the current device (NOA_DCS_ERROR_NOT_DEVICE_MEMORY). */
 int noa_dcs_mlp_infer(noa_dcs_mlp *model, const uint8_t *trust, int n_segments, const noa_dcs_element *elements,
                       const int64_t *counts, double mass, double *result, const double *K, const double *q,
                       float tolerance, unsigned long long *stats, void *stream);

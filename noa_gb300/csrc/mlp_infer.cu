@@ -37,6 +37,7 @@
 #include <cuda_runtime.h>
 
 #include <cstdio>
+#include <mutex>
 
 using namespace noa_mlp;
 
@@ -447,8 +448,22 @@ struct InferScratch {
     int64_t cap = 0;
     void *buf = nullptr;
 };
-InferScratch g_scratch;  // grown on demand; one per process (the inference call is not thread-safe)
+InferScratch g_scratch;  // grown on demand; one per process, guarded by g_scratch_mu
+std::mutex g_scratch_mu;
 thread_local char g_ierr[256] = "";
+
+// A buffer must be device (or managed) memory of the current device before it
+// reaches a kernel.
+bool on_device(const void *ptr, int device) {
+    if (!ptr)
+        return false;
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, ptr) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    return a.type == cudaMemoryTypeManaged || (a.type == cudaMemoryTypeDevice && a.device == device);
+}
 
 int ifail(int st, const char *msg, cudaError_t e = cudaSuccess) {
     if (e != cudaSuccess)
@@ -502,6 +517,10 @@ extern "C" int noa_dcs_mlp_infer(noa_dcs_mlp *model, const uint8_t *trust, int n
     // scratch: counters, then the two lists
     int dev = 0;
     cudaGetDevice(&dev);
+    if (!on_device(K, dev) || !on_device(q, dev) || !on_device(result, dev) || !on_device(trust, dev))
+        return ifail(NOA_DCS_ERROR_NOT_DEVICE_MEMORY, "K, q, result and the trust grid must be device memory");
+    // one call at a time owns the scratch (calls from several host threads serialise here)
+    std::lock_guard<std::mutex> lock(g_scratch_mu);
     const size_t per = sizeof(int32_t) + sizeof(float) + sizeof(float4) + 1 + sizeof(int32_t) + 1;
     if (g_scratch.device != dev || g_scratch.cap < n) {
         if (g_scratch.buf)
