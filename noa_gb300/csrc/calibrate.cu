@@ -40,6 +40,15 @@ extern "C" {
 int noa_dcs_probe_fma(int fp64, void *out, int blocks, int iters, double *flops, void *stream) {
     if (!out || blocks <= 0 || iters <= 0)
         return NOA_DCS_ERROR_INVALID_VALUE;
+    // out receives blocks x 256 values: it must be device memory of the current device
+    int dev = 0;
+    cudaPointerAttributes a;
+    if (cudaGetDevice(&dev) != cudaSuccess || cudaPointerGetAttributes(&a, out) != cudaSuccess) {
+        cudaGetLastError();
+        return NOA_DCS_ERROR_NOT_DEVICE_MEMORY;
+    }
+    if (!(a.type == cudaMemoryTypeManaged || (a.type == cudaMemoryTypeDevice && a.device == dev)))
+        return NOA_DCS_ERROR_NOT_DEVICE_MEMORY;
     if (fp64)
         fma_chains<double><<<blocks, 256, 0, (cudaStream_t)stream>>>((double *)out, iters, 0.999999, 1e-7);
     else

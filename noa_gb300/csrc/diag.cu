@@ -7,6 +7,8 @@
 #include "dcs_launch.h"
 #include "lean64.cuh"
 
+#include <initializer_list>
+
 namespace {
 
 __global__ void lean64_eval_kernel(int fn, const double *__restrict__ x, const double *__restrict__ y, double *out,
@@ -34,6 +36,17 @@ extern "C" int noa_dcs_lean64_eval(int fn, const double *x, const double *y, dou
         return NOA_DCS_ERROR_INVALID_VALUE;
     if (n == 0)
         return NOA_DCS_SUCCESS;
+    int dev = 0;
+    cudaGetDevice(&dev);
+    for (const void *ptr : {(const void *)x, (const void *)out, (const void *)(fn == 3 ? y : x)}) {
+        cudaPointerAttributes a;
+        if (cudaPointerGetAttributes(&a, ptr) != cudaSuccess) {
+            cudaGetLastError();
+            return NOA_DCS_ERROR_NOT_DEVICE_MEMORY;
+        }
+        if (!(a.type == cudaMemoryTypeManaged || (a.type == cudaMemoryTypeDevice && a.device == dev)))
+            return NOA_DCS_ERROR_NOT_DEVICE_MEMORY;
+    }
     const int64_t blocks = (n + 255) / 256;
     lean64_eval_kernel<<<(int)(blocks < 4096 ? blocks : 4096), 256, 0, (cudaStream_t)stream>>>(fn, x, y, out, n);
     return cudaGetLastError() == cudaSuccess ? NOA_DCS_SUCCESS : NOA_DCS_ERROR_CUDA;

@@ -22,6 +22,8 @@
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
+#include <initializer_list>
+
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -432,6 +434,27 @@ cudaError_t backward(noa_dcs_mlp *m, int M, cudaStream_t s) {
     return cudaGetLastError();
 }
 
+// Every buffer must be device (or managed) memory of the current device before
+// it reaches a kernel; nullptr passes (optional arguments are checked by the
+// callers).
+bool device_ok(std::initializer_list<const void *> ptrs) {
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess)
+        return false;
+    for (const void *p : ptrs) {
+        if (!p)
+            continue;
+        cudaPointerAttributes a;
+        if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+            cudaGetLastError();
+            return false;
+        }
+        if (!(a.type == cudaMemoryTypeManaged || (a.type == cudaMemoryTypeDevice && a.device == dev)))
+            return false;
+    }
+    return true;
+}
+
 } // namespace
 
 extern "C" {
@@ -531,6 +554,8 @@ int noa_dcs_mlp_prepare(int process, const double *K, const double *q, const uin
         return mfail(NOA_DCS_ERROR_INVALID_VALUE, "bad sizes");
     if (n == 0)
         return NOA_DCS_SUCCESS;
+    if (!K || !q || !elem || !Xraw || !R || !valid || !device_ok({K, q, elem, Xraw, R, valid}))
+        return mfail(NOA_DCS_ERROR_NOT_DEVICE_MEMORY, "K, q, elem, Xraw, R and valid must be device memory");
     noa_dcs_consts hc[16];
     float hlogA[16];
     for (int i = 0; i < n_elements; i++) {
@@ -572,6 +597,8 @@ int noa_dcs_mlp_train(noa_dcs_mlp *m, const float *X, const float *T, int64_t n,
     g_merr[0] = '\0';
     if (!m || !X || !T || !perm || n < m->batch || n_steps < 0)
         return mfail(NOA_DCS_ERROR_INVALID_VALUE, "bad training arguments (n must be at least one batch)");
+    if (!device_ok({X, T, perm, losses}))
+        return mfail(NOA_DCS_ERROR_NOT_DEVICE_MEMORY, "X, T, perm and losses must be device memory");
     cudaStream_t s = (cudaStream_t)stream;
     const int B = m->batch;
     const int64_t batches = n / B;
@@ -604,6 +631,8 @@ int noa_dcs_mlp_predict(noa_dcs_mlp *m, const float *X, float *out, int64_t n, v
     g_merr[0] = '\0';
     if (!m || (n > 0 && (!X || !out)) || n < 0)
         return mfail(NOA_DCS_ERROR_INVALID_VALUE, "bad arguments");
+    if (n > 0 && !device_ok({X, out}))
+        return mfail(NOA_DCS_ERROR_NOT_DEVICE_MEMORY, "X and out must be device memory");
     cudaStream_t s = (cudaStream_t)stream;
     for (int64_t off = 0; off < n; off += m->batch) {
         const int M = (int)((n - off) < m->batch ? (n - off) : m->batch);
@@ -620,6 +649,8 @@ int noa_dcs_mlp_gradient(noa_dcs_mlp *m, const float *X, const float *T, int n, 
     g_merr[0] = '\0';
     if (!m || !X || !T || !grad || n < 1 || n > m->batch)
         return mfail(NOA_DCS_ERROR_INVALID_VALUE, "bad arguments (1 <= n <= batch)");
+    if (!device_ok({X, T, grad, loss}))
+        return mfail(NOA_DCS_ERROR_NOT_DEVICE_MEMORY, "X, T, grad and loss must be device memory");
     cudaStream_t s = (cudaStream_t)stream;
     cudaMemcpyAsync(m->Xb, X, sizeof(float) * IN * n, cudaMemcpyDeviceToDevice, s);
     cudaMemcpyAsync(m->Tb, T, sizeof(float) * n, cudaMemcpyDeviceToDevice, s);
