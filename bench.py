@@ -493,6 +493,7 @@ def load_traffic():
 
 
 def run_ours(args):
+    import numpy as np
     import torch
     import torch.distributed as tdist
     from noa_gb300 import _lib
@@ -546,6 +547,22 @@ def run_ours(args):
                   for p, name in enumerate(PROCESSES)}
     elapsed = reduce_max(elapsed, world, dev)
     value = world * 4 * n * args.steps / elapsed
+
+    # parity of the timed outputs: a seeded sample of 1e5 pairs against the
+    # oracle (the reference's algorithm, bit-exact with it on the CPU)
+    parity = None
+    if rank == 0:
+        import oracle
+        idx = np.sort(np.random.default_rng(2024).choice(n, min(n, 100_000), replace=False))
+        ti = torch.from_numpy(idx).to(dev)
+        parity = {"sample": f"{len(idx)} seeded indices of the timed step's pairs"}
+        for p, name in enumerate(PROCESSES):
+            got = outs[p][ti].cpu().numpy()
+            ref = oracle.dcs(p, K[idx], q[idx], STANDARD_ROCK, MUON_MASS)
+            nz = ref != 0
+            rel = np.abs(got[nz] - ref[nz]) / np.abs(ref[nz]) if nz.any() else np.zeros(1)
+            parity[name] = {"mean_rel": float(rel.mean()), "max_rel": float(rel.max()),
+                            "zero_pattern_equal": bool(np.array_equal(got == 0, ref == 0))}
 
     # e2e: host buffers in pinned memory, through noa_dcs_vmap_host, copies timed.
     e2e = None
@@ -609,6 +626,8 @@ def run_ours(args):
         "clocks": clocks.summary(),
         "gpu_launches": 4 * args.steps,
     }
+    if parity is not None:
+        line["parity_vs_oracle"] = parity
     if not args.no_batched:
         line["batched"] = time_batched(torch, args)
     if not args.no_integrals:
