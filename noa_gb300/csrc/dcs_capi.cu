@@ -99,13 +99,13 @@ int launch(int process, int precision, double *result, const double *K, const do
 
 // ---------------------------------------------------------------- host path
 constexpr int64_t kChunk = (int64_t)1 << 21; // pairs per pipeline stage
-constexpr int kSlots = 2;
+constexpr int kSlots = 3;  // copy in, compute and copy out of three chunks overlap
 constexpr int kMaxDevices = 64;
 
 struct Staging {
     std::mutex mu;
     double *buf = nullptr; // kSlots x {K, q, out} x kChunk
-    cudaStream_t st[kSlots] = {nullptr, nullptr};
+    cudaStream_t st[kSlots] = {};
 };
 Staging g_staging[kMaxDevices];
 

@@ -33,6 +33,14 @@ constexpr int F_TILE = F_THREADS * F_ITEMS;
 constexpr int F_QCAP = F_TILE + F_THREADS;
 constexpr int F_RCAP = 2 * F_THREADS;
 
+// Resident CTAs per SM that each kernel is compiled for (its register budget
+// follows).  Measured on 1e7 pairs: pair production is fastest at 2 (3.5 ms
+// at 3, where it spills), photonuclear at 3; the short bodies fit 4.
+template <int PROC>
+constexpr int f32_min_ctas() {
+    return PROC == NOA_DCS_PROC_PPROD ? 2 : PROC == NOA_DCS_PROC_PHOTO ? 3 : 4;
+}
+
 template <int PROC>
 __device__ __forceinline__ double eval32(double K, double q, const noa_dcs_consts &c, float &est) {
     if (PROC == NOA_DCS_PROC_BREMS)
@@ -142,7 +150,7 @@ __device__ __forceinline__ void fp32_step(Queues &s, int e, bool valid, double *
 }
 
 template <int PROC>
-__global__ void __launch_bounds__(F_THREADS) dcs_fp32c_kernel(const double *__restrict__ K,
+__global__ void __launch_bounds__(F_THREADS, f32_min_ctas<PROC>()) dcs_fp32c_kernel(const double *__restrict__ K,
                                                               const double *__restrict__ q, double *out, int64_t n,
                                                               const noa_dcs_consts c, float tol) {
     __shared__ Queues s;

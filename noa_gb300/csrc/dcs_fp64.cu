@@ -44,6 +44,13 @@ constexpr int CMP_ITEMS = 4;
 constexpr int CMP_TILE = CMP_THREADS * CMP_ITEMS;
 constexpr int CMP_QCAP = CMP_TILE + CMP_THREADS;
 
+// Resident CTAs per SM that the compacting kernels are compiled for (the
+// register budget per thread follows).  Measured on 1e7 pairs: pair
+// production 13.8 ms at 2 (112 registers) against 18.5 ms at 3; photonuclear
+// 9.0 ms at 4 (64 registers) against 10.8 ms at 3.
+#define NOA_DCS_PPROD_MIN_CTAS 2
+#define NOA_DCS_PHOTO_MIN_CTAS 4
+
 template <int PROC>
 __device__ __forceinline__ double eval_fp64(double K, double q, const noa_dcs_consts &c) {
     if (PROC == NOA_DCS_PROC_BREMS)
@@ -112,7 +119,7 @@ __device__ __forceinline__ int block_exclusive_scan(int v, int *warp_tot, int *t
 }
 
 template <int PROC>
-__global__ void __launch_bounds__(CMP_THREADS, PROC == NOA_DCS_PROC_PHOTO ? 4 : 2) dcs_fp64_compact_kernel(const double *__restrict__ K,
+__global__ void __launch_bounds__(CMP_THREADS, PROC == NOA_DCS_PROC_PHOTO ? NOA_DCS_PHOTO_MIN_CTAS : NOA_DCS_PPROD_MIN_CTAS) dcs_fp64_compact_kernel(const double *__restrict__ K,
                                                                        const double *__restrict__ q, double *out,
                                                                        int64_t n, const noa_dcs_consts c) {
     __shared__ double qK[CMP_QCAP];
