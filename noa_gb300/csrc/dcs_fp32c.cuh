@@ -380,9 +380,10 @@ NOA_HD double photo_fp32c(double K, double q, const noa_dcs_consts &c, float &es
 }
 
 // ---------------------------------------------------------------- ionisation
-// The close-collision cross-section keeps FP64: its a1 + a2/q cancels by up to
-// gamma^2 near q = W_max (dcs.hh:427-431).  Only the radiative correction, a
-// relative term of O(1e-2), runs in FP32.
+// The close-collision cross-section's a1 + a2/q cancels by up to gamma^2 near
+// q = W_max as the reference writes it (dcs.hh:427-431); rearranged into
+// non-negative terms it runs in FP32, with only W_max, the bounds and W_max - q
+// in FP64.  The radiative correction, a relative term of O(1e-2), is FP32.
 NOA_HD double ion_fp32c(double K, double q, const noa_dcs_consts &c, float &est) {
     est = 0.f;
     const double mass = c.mass;
@@ -393,17 +394,25 @@ NOA_HD double ion_fp32c(double K, double q, const noa_dcs_consts &c, float &est)
         return 0.;
     if (q <= c.io_Wmin)
         return 0.;
-    const double inv_P2 = d_rcp(P2);
-    const double inv_q = d_rcp(q);
-    const double cs = c.io_cZA * E * (0.5 * inv_P2 + inv_q * (E * E * inv_P2 * inv_q - d_rcp(Wmax)));
+    // Close-collision term, dcs.hh:427-431, rearranged so that every term is
+    // non-negative for q <= W_max (E^2 = P2 + m^2):
+    //   a0 + (a1 + a2/q)/q = 0.5/P2 + ((W_max - q)/(q W_max) + m^2/(P2 q))/q.
+    // W_max - q is formed in double (q may sit an ulp below W_max); the rest
+    // is float, ~10 roundings of same-sign terms.
+    const float qf = fpconv::f32(q), P2f = fpconv::f32(P2), Wf = fpconv::f32(Wmax);
+    const float dW = fpconv::f32(Wmax - q), m2f = fpconv::f32(mass * mass);
+    const float iq = f_rcp(qf), iP2 = f_rcp(P2f);
+    const float bracket = 0.5f * iP2 + iq * (dW * iq * f_rcp(Wf) + m2f * iP2 * iq);
+    const float csf = fpconv::f32(c.io_cZA) * fpconv::f32(E) * bracket;
     float Delta = 0.f;
     if (K >= c.io_k_rad) {
         const float L1 = log1pf(fpconv::f32(q * (2. / ME)));
         const float Ef = fpconv::f32(E);
         Delta = 1.16141E-03f * L1 * (logf(4.f * Ef * fpconv::f32(E - q) * fpconv::f32(c.inv_m2)) - L1);
     }
-    est = fabsf(Delta) * 8.f * U32;  // the float part is Delta, relative to 1 + Delta
-    return cs * (1. + fpconv::f64(Delta));
+    // the close-collision term (max observed 8.7 u) and Delta relative to 1 + Delta
+    est = (12.f + fabsf(Delta) * 8.f) * U32;
+    return fpconv::f64(csf) * (1. + fpconv::f64(Delta));
 }
 
 } // namespace noa_dcs
