@@ -84,6 +84,40 @@ NOA_HD void f_exp_split(double u, float &e, float &em1) {
     em1 = fmaf(eh, ul, expm1f(uh));
 }
 
+// The same for u = x t with x a double literal and t = th + tl a float-float
+// pair, entirely in FP32: x = xh + xl is split at compile time or in the
+// integer pipe, x t is formed as a float-float product (the FMA gives xh th
+// exactly), so exp sees u to ~2^-48 without an FP64 instruction.
+NOA_HD void f_exp_split_ff(double x, float th, float tl, float &e, float &em1) {
+    const float xh = fpconv::f32(x);
+    const float xl = fpconv::f32(x - fpconv::f64(xh));
+    const float ph = xh * th;
+    const float pl = fmaf(xh, th, -ph) + (xh * tl + xl * th);
+    const float uh = ph + pl;
+    const float ul = pl - (uh - ph);
+    const float eh = expf(uh);
+    e = fmaf(eh, ul, eh);
+    em1 = fmaf(eh, ul, expm1f(uh));
+}
+
+// exp(c + h x) and expm1 of it, with c = ch + cl and h = hh + hl float-float
+// pairs and x a double literal, entirely in FP32 (as f_exp_split_ff).
+NOA_HD void f_exp_split_aff(float ch, float cl, float hh, float hl, double x, float &e, float &em1) {
+    const float xh = fpconv::f32(x);
+    const float xl = fpconv::f32(x - fpconv::f64(xh));
+    const float ph = hh * xh;
+    const float pl = fmaf(hh, xh, -ph) + (hh * xl + hl * xh);
+    // (ch + ph) as a float-float sum, then the low parts
+    const float s = ch + ph;
+    const float bb = s - ch;
+    const float sl = (ch - (s - bb)) + (ph - bb) + (cl + pl);
+    const float uh = s + sl;
+    const float ul = sl - (uh - s);
+    const float eh = expf(uh);
+    e = fmaf(eh, ul, eh);
+    em1 = fmaf(eh, ul, expm1f(uh));
+}
+
 // ---------------------------------------------------------------- bremsstrahlung
 NOA_HD double brems_fp32c(double K, double q, const noa_dcs_consts &c, float &est) {
     est = 0.f;
@@ -147,6 +181,7 @@ NOA_HD double pprod_fp32c(double K, double q, const noa_dcs_consts &c, float &es
     const double beta_d = 0.5 * q * q * d_rcp(E * Emq);
     const double tmin_d = d_log(argmin);
     const float tmin = fpconv::f32(tmin_d);
+    const float tmin_lo = fpconv::f32(tmin_d - fpconv::f64(tmin));  // tmin = tmin + tmin_lo to ~2^-48
     const float beta = fpconv::f32(beta_d);
     const float xi_factor = fpconv::f32(c.pp_half_r2 * beta_d);
     const float qf = fpconv::f32(q);
@@ -164,7 +199,7 @@ NOA_HD double pprod_fp32c(double K, double q, const noa_dcs_consts &c, float &es
 #pragma unroll
     for (int j = 0; j < 8; j++) {
         float eps, rho;
-        f_exp_split(GL8Xd[j] * tmin_d, eps, rho);
+        f_exp_split_ff(GL8Xd[j], tmin, tmin_lo, eps, rho);
         rho = -rho;
         const float rho2 = rho * rho;
         const float rho21 = eps * (2.f - eps);
@@ -238,18 +273,36 @@ NOA_HD double pprod_fp32c(double K, double q, const noa_dcs_consts &c, float &es
     }
 
     const double gamma = 1. + K * c.inv_mass;
-    float zeta = 0.f;
+    // zeta (dcs.hh:230-251) in float, with a bound on its float error; where
+    // the cancellations in its numerator or denominator make that bound
+    // matter (above 1e-7 of Z + zeta, e.g. for hydrogen), it is recomputed in
+    // FP64 as in the plain kernel
+    float zeta = 0.f, zeta_err = 0.f;
     if (!(gamma <= 35.)) {
         const float gf = fpconv::f32(gamma), Z13 = fpconv::f32(c.pp_Z13);
-        zeta = 0.073f * logf(gf * f_rcp(1.f + fpconv::f32(c.pp_gamma1) * gf * Z13 * Z13)) - 0.26f;
-        if (zeta <= 0.f)
+        const float L1 = logf(gf * f_rcp(1.f + fpconv::f32(c.pp_gamma1) * gf * Z13 * Z13));
+        zeta = 0.073f * L1 - 0.26f;
+        if (zeta <= 0.f) {
             zeta = 0.f;
-        else
-            zeta = f_div(zeta, 0.058f * logf(gf * f_rcp(1.f + fpconv::f32(c.pp_gamma2) * gf * Z13)) - 0.14f);
+        } else {
+            const float L2 = logf(gf * f_rcp(1.f + fpconv::f32(c.pp_gamma2) * gf * Z13));
+            const float den = 0.058f * L2 - 0.14f;
+            const float ez = ((0.073f * (fabsf(L1) + 3.f) + 0.26f) * f_rcp(zeta) +
+                              (0.058f * (fabsf(L2) + 3.f) + 0.14f) * f_rcp(fabsf(den)) + 2.f) * U32;
+            zeta = f_div(zeta, den);
+            zeta_err = fabsf(zeta) * ez;
+            if (!(zeta_err <= 1e-7f * (fpconv::f32(c.Zd) + zeta))) {
+                double zd = 0.073 * d_log(gamma * d_rcp(1. + c.pp_gamma1 * gamma * c.pp_Z13 * c.pp_Z13)) - 0.26;
+                zd = zd <= 0. ? 0. : zd * d_rcp(0.058 * d_log(gamma * d_rcp(1. + c.pp_gamma2 * gamma * c.pp_Z13)) - 0.14);
+                zeta = fpconv::f32(zd);
+                zeta_err = fabsf(zeta) * U32;
+            }
+        }
         edge |= fabsf(gf - 35.f) < 1e-4f;
     }
     const double Id = I.value();
-    est = edge ? INFINITY : 1.3f * err * f_rcp(fpconv::f32(fabs(Id)));  // calibrated: max error <= est
+    // calibrated: max error <= est over 4e6 seeded pairs for each of the 10 elements
+    est = edge ? INFINITY : 1.3f * err * f_rcp(fpconv::f32(fabs(Id))) + zeta_err * f_rcp(fpconv::f32(c.Zd) + zeta);
     const double dcs = c.pp_cZ * (c.Zd + fpconv::f64(zeta)) * Emq * Id * d_rcp(q * E);
     return (dcs < 0.) ? 0. : dcs * (mass + K) * c.scale_A;
 }
@@ -284,6 +337,9 @@ NOA_HD double photo_fp32c(double K, double q, const noa_dcs_consts &c, float &es
     const float inv_Mq = 2.f * inv_2Mq;
     const float Q2maxf = fpconv::f32(Q2max);
     const float half_dp = fpconv::f32(0.5 * dpQ2);
+    // node abscissae log Q2 = pQ2c + (dpQ2 / 2) x_j in float-float
+    const float pc_h = fpconv::f32(pQ2c), pc_l = fpconv::f32(pQ2c - fpconv::f64(pc_h));
+    const float hd_h = half_dp, hd_l = fpconv::f32(0.5 * dpQ2 - fpconv::f64(hd_h));
 
     const float m02 = 0.31985f, mP2 = 49.457f, mR2 = 0.15052f;
     const float cP1 = 0.28067f, cP2 = 0.22291f, cP3 = 2.1979f;
@@ -316,7 +372,7 @@ NOA_HD double photo_fp32c(double K, double q, const noa_dcs_consts &c, float &es
 #pragma unroll
     for (int j = 0; j < 9; j++) {
         float Q2, unused;
-        f_exp_split(pQ2c + 0.5 * dpQ2 * GL9Xd[j], Q2, unused);
+        f_exp_split_aff(pc_h, pc_l, hd_h, hd_l, GL9Xd[j], Q2, unused);
         const float invQ2 = f_rcp(Q2);
         const float x = 0.5f * Q2 * inv_Mq;
         // ALLM, dcs.hh:288-306
