@@ -124,7 +124,7 @@ __device__ __forceinline__ double pprod_fp64(double K, double q, const noa_dcs_c
     const double b2 = 2. * beta, b15 = 1.5 * beta, b3 = 3. * beta, b4 = 4. * beta;
 
     double I = 0.;
-#pragma unroll
+#pragma unroll 1  // rolled: 1% faster than unrolled on GB300 (smaller code, same FP64 work)
     for (int j = 0; j < 8; j++) {
         const double eps = lean_exp(kGL8X[j] * tmin);
         const double rho = 1. - eps;
