@@ -106,3 +106,17 @@ def test_fp32c_large_size(cuda_device, process):
     idx = np.random.default_rng(12).choice(n, 200_000, replace=False)
     s = rel_stats(a.cpu().numpy()[idx], oracle.dcs(process, K[idx], q[idx], STANDARD_ROCK, MUON_MASS))
     assert s["zero_agree"] and s["max"] <= TOL, s
+
+
+@pytest.mark.parametrize("z", sorted(ELEMENTS))
+def test_fp32c_pair_production_every_element(cuda_device, z):
+    """The pair-production error estimate across all ten elements on 2e6
+    pairs each: hydrogen's zeta (comparable to Z, with cancelling numerator
+    and denominator) once let a pair through at 1.03e-6."""
+    K, q = kinetic_recoil(2_000_000, offset=(50 + z) << 22)
+    el = ELEMENTS[z]
+    got = fp32c(1, K, q, el)
+    exp = oracle.dcs(1, K, q, el, MUON_MASS)
+    s = rel_stats(got, exp)
+    assert s["zero_agree"] and s["nonfinite_agree"]
+    assert s["max"] <= TOL, s
