@@ -77,6 +77,10 @@ typedef struct noa_dcs_consts {
     double io_Wmin;         /* 0.62 I */
     double io_k_rad;        /* 0.5 m1 m1 / me, radiative-correction threshold */
     double io_cZA;          /* 1.535336e-5 Z / A */
+
+    /* 1 / mass as a float pair (hi + lo to ~2^-48), for float-float arithmetic */
+    float inv_mass_h;
+    float inv_mass_l;
 } noa_dcs_consts;
 
 /* Fills c from (A, I, Z, mass) with the reference's expressions (host code;
@@ -90,6 +94,8 @@ static inline void noa_dcs_fill_consts(noa_dcs_consts *c, double A, double I, in
     c->Z = Z;
     c->Zd = (double)Z;
     c->inv_mass = 1. / mass;
+    c->inv_mass_h = (float)c->inv_mass;
+    c->inv_mass_l = (float)(c->inv_mass - (double)c->inv_mass_h);
     c->inv_m2 = 1. / (mass * mass);
     c->scale_A = 1E+03 * NOA_AVOGADRO_NUMBER / A;
     { // physics.hh:121-133
