@@ -159,8 +159,9 @@ __global__ void __launch_bounds__(256) fallback_kernel(const __grid_constant__ I
             sg = p.fb_seg[e];
             const noa_dcs_consts &c = p.consts[sg];
             float est;
-            const double v = PROC == NOA_DCS_PAIR_PRODUCTION ? noa_dcs::pprod_fp32c<true>(p.K[i], p.q[i], c, est)
-                                                             : noa_dcs::photo_fp32c<true>(p.K[i], p.q[i], c, est);
+            // classify_kernel listed only pairs that the exact bounds leave open
+            const double v = PROC == NOA_DCS_PAIR_PRODUCTION ? noa_dcs::pprod_fp32c<false>(p.K[i], p.q[i], c, est)
+                                                             : noa_dcs::photo_fp32c<false>(p.K[i], p.q[i], c, est);
             redo = !(est <= p.tol);
             if (!redo)
                 p.out[i] = v;
