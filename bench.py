@@ -55,6 +55,7 @@ def parse_args():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-batched", action="store_true")
+    ap.add_argument("--no-mixed-1e8", action="store_true")
     ap.add_argument("--no-integrals", action="store_true")
     ap.add_argument("--no-surrogate", action="store_true")
     ap.add_argument("--surrogate-queries", type=int, default=100_000_000)
@@ -272,6 +273,62 @@ def time_fp32c(lib, torch, tk, tq, ref_outs, n, el, mass, stream, args, fp64_s):
     total = sum(v["ms_per_launch"] for v in res.values())
     res["all_processes"] = {"evals_per_s": 4 * n / (total * 1e-3),
                             "speedup_vs_fp64": sum(fp64_s.values()) / args.steps / (total * 1e-3)}
+    return res
+
+
+def time_mixed_1e8(torch, args):
+    """The mixed-precision target workload: 1e8 seeded pairs of standard rock,
+    each process in plain FP64 and in FP32C (tolerance 1e-6) on the same
+    pairs: ms per launch, speed-up, the FP32C error against FP64, and the
+    FP64 output against the oracle on a seeded sample of 1e5 of the pairs."""
+    from noa_gb300 import _lib
+    from noa_gb300.elements import MUON_MASS, STANDARD_ROCK
+    from noa_gb300.workload import kinetic_recoil
+    import numpy as np
+    import oracle
+    n = 100_000_000
+    K, q = kinetic_recoil(n, offset=1 << 33)
+    tk, tq = torch.from_numpy(K).cuda(), torch.from_numpy(q).cuda()
+    idx = np.sort(np.random.default_rng(7).choice(n, 100_000, replace=False))
+    Ks, qs = K[idx], q[idx]
+    del K, q
+    o64, o32 = torch.empty_like(tk), torch.empty_like(tk)
+    lib = _lib.load()
+    el = _lib.element_struct(STANDARD_ROCK)
+    stream = torch.cuda.current_stream()
+    res = {"n_pairs": n, "element": "standard rock", "tolerance": 1e-6}
+    reps = max(1, min(args.steps, 2))
+    tot64 = tot32 = 0.0
+    for p, name in enumerate(PROCESSES):
+        ms = {}
+        for prec, out in ((0, o64), (1, o32)):
+            def launch():
+                _lib.check(lib.noa_dcs_cuda_vmap(p, prec, out.data_ptr(), tk.data_ptr(), tq.data_ptr(), n, el,
+                                                 MUON_MASS, stream.cuda_stream))
+            launch()
+            s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            torch.cuda.synchronize()
+            s.record(stream)
+            for _ in range(reps):
+                launch()
+            e.record(stream)
+            torch.cuda.synchronize()
+            ms[prec] = s.elapsed_time(e) / reps
+        tot64 += ms[0]
+        tot32 += ms[1]
+        # the FP64 output against the oracle on a seeded sample of the 1e8 pairs
+        ref = oracle.dcs(p, Ks, qs, STANDARD_ROCK, MUON_MASS)
+        got = o64[torch.from_numpy(idx).to(o64.device)].cpu().numpy()
+        nz = ref != 0
+        rel = np.abs(got[nz] - ref[nz]) / np.abs(ref[nz]) if nz.any() else np.zeros(1)
+        res[name] = {"fp64_ms": ms[0], "fp32c_ms": ms[1], "speedup": ms[0] / ms[1],
+                     "fp32c_evals_per_s": n / (ms[1] * 1e-3), **rel_error_stats(torch, o32, o64),
+                     "fp64_vs_oracle_sample": {"mean_rel": float(rel.mean()), "max_rel": float(rel.max()),
+                                               "zero_pattern_equal": bool(np.array_equal(got == 0, ref == 0))}}
+    res["all_processes"] = {"fp64_evals_per_s": 4 * n / (tot64 * 1e-3), "fp32c_evals_per_s": 4 * n / (tot32 * 1e-3),
+                            "speedup": tot64 / tot32}
+    del tk, tq, o64, o32
+    torch.cuda.empty_cache()
     return res
 
 
@@ -628,6 +685,8 @@ def run_ours(args):
     }
     if parity is not None:
         line["parity_vs_oracle"] = parity
+    if not args.no_mixed_1e8 and world == 1:
+        line["mixed_precision_1e8"] = time_mixed_1e8(torch, args)
     if not args.no_batched:
         line["batched"] = time_batched(torch, args)
     if not args.no_integrals:
