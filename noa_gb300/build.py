@@ -7,7 +7,7 @@ Products (all git-ignored, built in place):
     noa_gb300/libnoa_dcs.so      CUDA kernels + C ABI of include/noa_dcs.h, sm_103a only
     noa_gb300/libnoa_dcs_torch.so  LibTorch drop-in (include/noa_gb300/dcs_cuda.hh)
     noa_gb300/_muons_cuda*.so    Python module mirroring the reference notebook's extension
-    oracle/liboracle_dcs.so      CPU restatement used by the tests as the checker
+    oracle/liboracle_dcs.so      CPU restatement of the reference, the tests' oracle
     oracle/_ref/libnoa_ref_dcs.so  the reference's own dcs.hh (only where a noa checkout exists)
 
 Each .cu file is compiled in its own nvcc process, in parallel, then linked.

@@ -4,8 +4,9 @@
  * This header restates, in scalar C++, the four differential cross-sections of
  * NOA (grinisrit/noa) in the reference's operation order, so that compiled
  * with IEEE semantics (-O2 -ffp-contract=off, no fast-math) it reproduces the
- * reference's own CPU output bit for bit.  It is the checker for the CUDA
- * kernels in noa_gb300/csrc; it is never linked into the product library.
+ * reference's own CPU output bit for bit.  The tests compare the CUDA
+ * kernels in noa_gb300/csrc with it; it is never linked into the product
+ * library.
  * Only tests/, __graft_entry__.smoke() and bench.py's CPU baseline use it.
  *
  * Every function is templated on the scalar type so that the same source can
