@@ -78,9 +78,11 @@ typedef struct noa_dcs_consts {
     double io_k_rad;        /* 0.5 m1 m1 / me, radiative-correction threshold */
     double io_cZA;          /* 1.535336e-5 Z / A */
 
-    /* 1 / mass as a float pair (hi + lo to ~2^-48), for float-float arithmetic */
-    float inv_mass_h;
-    float inv_mass_l;
+    /* float pairs (hi + lo to ~2^-48) for float-float arithmetic */
+    float inv_mass_h, inv_mass_l;  /* 1 / mass */
+    float mass_h, mass_l;          /* mass */
+    float io_cm_h, io_cm_l;        /* (mass + me)^2: W_max = 2 me K (K + 2 mass) / ((mass + me)^2 + 2 me K) */
+    float mass2_f;                 /* mass^2 rounded to float */
 } noa_dcs_consts;
 
 /* Fills c from (A, I, Z, mass) with the reference's expressions (host code;
@@ -96,6 +98,14 @@ static inline void noa_dcs_fill_consts(noa_dcs_consts *c, double A, double I, in
     c->inv_mass = 1. / mass;
     c->inv_mass_h = (float)c->inv_mass;
     c->inv_mass_l = (float)(c->inv_mass - (double)c->inv_mass_h);
+    c->mass_h = (float)mass;
+    c->mass_l = (float)(mass - (double)c->mass_h);
+    {
+        const double cm = (mass + me) * (mass + me);
+        c->io_cm_h = (float)cm;
+        c->io_cm_l = (float)(cm - (double)c->io_cm_h);
+    }
+    c->mass2_f = (float)(mass * mass);
     c->inv_m2 = 1. / (mass * mass);
     c->scale_A = 1E+03 * NOA_AVOGADRO_NUMBER / A;
     { // physics.hh:121-133

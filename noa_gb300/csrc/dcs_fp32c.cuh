@@ -501,39 +501,93 @@ NOA_HD double photo_fp32c(double K, double q, const noa_dcs_consts &c, float &es
 }
 
 // ---------------------------------------------------------------- ionisation
+// The bit pattern of x as a signed integer: positive doubles order as these do.
+NOA_HD long long dbits(double x) {
+#if defined(__CUDA_ARCH__)
+    return __double_as_longlong(x);
+#else
+    long long b;
+    memcpy(&b, &x, sizeof b);
+    return b;
+#endif
+}
+
+// x = h + l to 2^-47 relative: h is x truncated to 24 significant bits and l
+// the rest rounded to float.  Integer and FP32 operations only on the device
+// (ff_from takes an FP64 subtraction).  Requires 2^-74 <= x < 2^127.
+NOA_HD FF ff_split(double x) {
+#if defined(__CUDA_ARCH__)
+    const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+    const unsigned e = (unsigned)(b >> 52);
+    const float h = __uint_as_float(((unsigned)(b >> 29) & 0x007FFFFFu) | ((e - 896u) << 23));
+    const float scale = __uint_as_float((e - 948u) << 23);  // 2^(e - 1075), the weight of bit 0
+    return FF{h, __uint2float_rn((unsigned)b & 0x1FFFFFFFu) * scale};
+#else
+    unsigned long long b;
+    memcpy(&b, &x, sizeof b);
+    b &= ~0x1FFFFFFFull;
+    double t;
+    memcpy(&t, &b, sizeof t);
+    return FF{(float)t, (float)(x - t)};
+#endif
+}
+
+// W_max = 2 me P2 / (m^2 + me (me + 2E)) of dcs.hh:415-419 equals
+// 2 me K (K + 2m) / ((m + me)^2 + 2 me K) (E = K + m); every term is positive,
+// so float-float keeps it to ~1e-13 relative.
+constexpr float kTwoMeH = (float)(2. * ME);
+constexpr float kTwoMeL = (float)(2. * ME - (double)kTwoMeH);
+
+// The reference's three zero conditions (dcs.hh:420-424) are decided from a
+// float-float W_max where they are clear by a relative margin of 1e-5, and by
+// the FP64 redo (est = infinity) inside the margin, so the zero pattern is
+// the reference's.  q <= 0.62 I is an exact integer compare of bit patterns.
+//
 // The close-collision cross-section's a1 + a2/q cancels by up to gamma^2 near
 // q = W_max as the reference writes it (dcs.hh:427-431); rearranged into
-// non-negative terms it runs in FP32, with only W_max, the bounds and W_max - q
-// in FP64.  The radiative correction, a relative term of O(1e-2), is FP32.
+// non-negative terms it runs in FP32, with W_max - q from the float-float
+// W_max (q >= 1e-5 below it, so to ~1e-8 relative).  The radiative
+// correction, a relative term of O(1e-2), is FP32, with E - q in FP64.
 NOA_HD double ion_fp32c(double K, double q, const noa_dcs_consts &c, float &est) {
     est = 0.f;
-    const double mass = c.mass;
-    const double P2 = K * (K + 2. * mass);
-    const double E = K + mass;
-    const double Wmax = ion_wmax(P2, E, c);
-    if ((Wmax < NOA_X_FRACTION * K) || (q > Wmax))
+    const long long qb = dbits(q);
+    if (qb >= 0 && qb <= dbits(c.io_Wmin))  // +0 <= q <= Wmin
         return 0.;
-    if (q <= c.io_Wmin)
+    const float Kf = fpconv::f32(K), qf = fpconv::f32(q);
+    if (!(Kf > 1e-20f && Kf < 1e12f && qf > 1e-20f && qf < 1e12f)) {  // NaN, q < 0, extreme ranges
+        est = INFINITY;
         return 0.;
+    }
+    const FF Kx = ff_split(K), qx = ff_split(q);
+    const FF two_me{kTwoMeH, kTwoMeL};
+    const FF P2 = ff_mul(Kx, ff_add(Kx, FF{2.f * c.mass_h, 2.f * c.mass_l}));
+    const FF W = ff_div(ff_mul(two_me, P2), ff_add(FF{c.io_cm_h, c.io_cm_l}, ff_mul(two_me, Kx)));
+    const FF dW = ff_add(W, ff_neg(qx));
+    constexpr float margin = 1e-5f;
+    const float XK = (float)NOA_X_FRACTION * Kf;
+    if (W.h < XK * (1.f - margin) || dW.h < -margin * qf)  // W_max < X K, or q > W_max
+        return 0.;
+    if (!(W.h > XK * (1.f + margin) && dW.h > margin * qf)) {  // within the margin of a bound
+        est = INFINITY;
+        return 0.;
+    }
     // Close-collision term, dcs.hh:427-431, rearranged so that every term is
     // non-negative for q <= W_max (E^2 = P2 + m^2):
     //   a0 + (a1 + a2/q)/q = 0.5/P2 + ((W_max - q)/(q W_max) + m^2/(P2 q))/q.
-    // W_max - q is formed in double (q may sit an ulp below W_max); the rest
-    // is float, ~10 roundings of same-sign terms.
-    const float qf = fpconv::f32(q), P2f = fpconv::f32(P2), Wf = fpconv::f32(Wmax);
-    const float dW = fpconv::f32(Wmax - q), m2f = fpconv::f32(mass * mass);
-    const float iq = f_rcp(qf), iP2 = f_rcp(P2f);
-    const float bracket = 0.5f * iP2 + iq * (dW * iq * f_rcp(Wf) + m2f * iP2 * iq);
-    const float csf = fpconv::f32(c.io_cZA) * fpconv::f32(E) * bracket;
+    const float iq = f_rcp(qf), iP2 = f_rcp(P2.h);
+    const float bracket = 0.5f * iP2 + iq * (dW.h * iq * f_rcp(W.h) + c.mass2_f * iP2 * iq);
+    const double E = K + c.mass;
+    const float Ef = fpconv::f32(E);
+    float cs = fpconv::f32(c.io_cZA) * Ef * bracket;
     float Delta = 0.f;
-    if (K >= c.io_k_rad) {
-        const float L1 = log1pf(fpconv::f32(q * (2. / ME)));
-        const float Ef = fpconv::f32(E);
+    if (dbits(K) >= dbits(c.io_k_rad)) {  // K >= k_rad, both positive
+        const float L1 = log1pf(qf * (float)(2. / ME));
         Delta = 1.16141E-03f * L1 * (logf(4.f * Ef * fpconv::f32(E - q) * fpconv::f32(c.inv_m2)) - L1);
+        cs *= 1.f + Delta;
     }
     // the close-collision term (max observed 8.7 u) and Delta relative to 1 + Delta
-    est = (12.f + fabsf(Delta) * 8.f) * U32;
-    return fpconv::f64(csf) * (1. + fpconv::f64(Delta));
+    est = (13.f + fabsf(Delta) * 8.f) * U32;
+    return fpconv::f64(cs);
 }
 
 } // namespace noa_dcs

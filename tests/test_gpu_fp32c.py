@@ -120,3 +120,30 @@ def test_fp32c_pair_production_every_element(cuda_device, z):
     s = rel_stats(got, exp)
     assert s["zero_agree"] and s["nonfinite_agree"]
     assert s["max"] <= TOL, s
+
+
+@pytest.mark.parametrize("z", [1, 11, 82])
+def test_fp32c_ionisation_bounds(cuda_device, z):
+    """Ionisation decides W_max < X K, q > W_max and q <= 0.62 I from a
+    float-float W_max with a relative margin of 1e-5, and in FP64 inside it:
+    pairs within 1e-16..1e-1 of W_max (both sides), around W_max = X K, at
+    0.62 I and across the radiative-correction threshold K = m^2 / (2 me)."""
+    rng = np.random.default_rng(40 + z)
+    el = ELEMENTS[z] if z != 11 else STANDARD_ROCK
+    me, m = 0.510998910e-03, MUON_MASS
+    n = 400_000
+    K1 = 10 ** rng.uniform(-3, 11, n)
+    E = K1 + m
+    W = 2 * me * K1 * (K1 + 2 * m) / (m * m + me * (me + 2 * E))
+    q1 = W * (1 + rng.choice([-1.0, 1.0], n) * 10 ** rng.uniform(-16, -1, n))
+    K2 = 10 ** rng.uniform(-1, 1, n)  # W_max = 0.05 K near K ~ 0.3 GeV
+    q2 = K2 * rng.uniform(0.0, 0.06, n)
+    wmin = 0.62 * el.I
+    K3 = 10 ** rng.uniform(0, 2, n)  # k_rad ~ 10.9 GeV for the muon
+    q3 = np.where(rng.random(n) < 0.5, wmin * (1 + rng.integers(-3, 4, n) * 2.0 ** -52), 10 ** rng.uniform(-7, 0, n))
+    for K, q in ((K1, q1), (K2, q2), (K3, q3)):
+        got = fp32c(3, K, q, el)
+        exp = oracle.dcs(3, K, q, el, MUON_MASS)
+        s = rel_stats(got, exp)
+        assert s["zero_agree"] and s["nonfinite_agree"], s
+        assert s["max"] <= TOL, s
