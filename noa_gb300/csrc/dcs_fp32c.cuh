@@ -149,47 +149,6 @@ NOA_HD void f_exp_split_aff(float ch, float cl, float hh, float hl, float xh, fl
     em1 = fmaf(eh, ul, expm1f(uh));
 }
 
-// ---------------------------------------------------------------- float-float
-// Unevaluated sums h + l of two floats (Dekker / Knuth error-free transforms
-// with FMA), ~2^-44 relative over a short expression: double-like accuracy on
-// the FP32 pipe.  from() and to_double() take one FP64 instruction each.
-struct FF {
-    float h, l;
-};
-NOA_HD FF ff_from(double x) {
-    const float h = fpconv::f32(x);
-    return FF{h, fpconv::f32(x - fpconv::f64(h))};
-}
-NOA_HD double ff_to_double(FF a) { return fpconv::f64(a.h) + fpconv::f64(a.l); }
-NOA_HD FF ff_norm(float s, float e) {  // |s| >= |e|
-    const float h = s + e;
-    return FF{h, e - (h - s)};
-}
-NOA_HD FF ff_add(FF a, FF b) {
-    const float s = a.h + b.h;
-    const float bb = s - a.h;
-    const float e = (a.h - (s - bb)) + (b.h - bb) + (a.l + b.l);
-    return ff_norm(s, e);
-}
-NOA_HD FF ff_add(float a, FF b) { return ff_add(FF{a, 0.f}, b); }
-NOA_HD FF ff_neg(FF a) { return FF{-a.h, -a.l}; }
-NOA_HD FF ff_mul(FF a, FF b) {
-    const float p = a.h * b.h;
-    const float e = fmaf(a.h, b.h, -p) + (a.h * b.l + a.l * b.h);
-    return ff_norm(p, e);
-}
-NOA_HD FF ff_mul(float a, FF b) { return ff_mul(FF{a, 0.f}, b); }
-NOA_HD FF ff_div(FF a, FF b) {
-    const float q1 = a.h / b.h;
-    const FF r = ff_add(a, ff_neg(ff_mul(FF{q1, 0.f}, b)));
-    return ff_norm(q1, r.h / b.h);
-}
-NOA_HD FF ff_sqrt(FF a) {
-    const float s = sqrtf(a.h);
-    const float r = fmaf(-s, s, a.h) + a.l;  // a - s^2, exact to the rounding of a.l
-    return ff_norm(s, r / (2.f * s));
-}
-
 // ---------------------------------------------------------------- bremsstrahlung
 NOA_HD double brems_fp32c(double K, double q, const noa_dcs_consts &c, float &est) {
     est = 0.f;
@@ -241,17 +200,7 @@ NOA_HD double pprod_fp32c(double K, double q, const noa_dcs_consts &c, float &es
         if ((argmin >= 1.) || (argmin <= 0.))
             return 0.;
     } else {
-        // argmin (dcs.hh:169-176) in float-float: ~2^-44 relative with four
-        // FP64 instructions (the splits) instead of ~25
-        const FF im{c.inv_mass_h, c.inv_mass_l};
-        const FF gamma = ff_add(1.f, ff_mul(ff_from(K), im));
-        const FF gmq = ff_add(1.f, ff_mul(ff_from(K - q), im));  // gamma - q/m
-        const FF x0 = ff_div(ff_from(4. * ME), ff_from(q));
-        const FF x1 = ff_div(FF{6.f, 0.f}, ff_mul(gamma, gmq));
-        const FF omx0 = ff_add(1.f, ff_neg(x0));
-        const FF num = ff_add(x0, ff_mul(ff_mul(2.f, omx0), x1));
-        const FF den = ff_add(1.f, ff_mul(ff_add(1.f, ff_neg(x1)), ff_sqrt(omx0)));
-        argmin = ff_to_double(ff_div(num, den));
+        argmin = ff_to_double(pprod_argmin_ff(K, q, c));
     }
     const double mass = c.mass;
     const double E = K + mass;
@@ -501,37 +450,6 @@ NOA_HD double photo_fp32c(double K, double q, const noa_dcs_consts &c, float &es
 }
 
 // ---------------------------------------------------------------- ionisation
-// The bit pattern of x as a signed integer: positive doubles order as these do.
-NOA_HD long long dbits(double x) {
-#if defined(__CUDA_ARCH__)
-    return __double_as_longlong(x);
-#else
-    long long b;
-    memcpy(&b, &x, sizeof b);
-    return b;
-#endif
-}
-
-// x = h + l to 2^-47 relative: h is x truncated to 24 significant bits and l
-// the rest rounded to float.  Integer and FP32 operations only on the device
-// (ff_from takes an FP64 subtraction).  Requires 2^-74 <= x < 2^127.
-NOA_HD FF ff_split(double x) {
-#if defined(__CUDA_ARCH__)
-    const unsigned long long b = (unsigned long long)__double_as_longlong(x);
-    const unsigned e = (unsigned)(b >> 52);
-    const float h = __uint_as_float(((unsigned)(b >> 29) & 0x007FFFFFu) | ((e - 896u) << 23));
-    const float scale = __uint_as_float((e - 948u) << 23);  // 2^(e - 1075), the weight of bit 0
-    return FF{h, __uint2float_rn((unsigned)b & 0x1FFFFFFFu) * scale};
-#else
-    unsigned long long b;
-    memcpy(&b, &x, sizeof b);
-    b &= ~0x1FFFFFFFull;
-    double t;
-    memcpy(&t, &b, sizeof t);
-    return FF{(float)t, (float)(x - t)};
-#endif
-}
-
 // W_max = 2 me P2 / (m^2 + me (me + 2E)) of dcs.hh:415-419 equals
 // 2 me K (K + 2m) / ((m + me)^2 + 2 me K) (E = K + m); every term is positive,
 // so float-float keeps it to ~1e-13 relative.

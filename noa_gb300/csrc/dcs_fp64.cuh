@@ -98,11 +98,23 @@ __device__ __forceinline__ bool pprod_live(double K, double q, const noa_dcs_con
     const float gamma = 1.f + fpconv::f32(K) * im;
     const float x1 = 6.f * lean64::rcp_approx(gamma * (1.f + fpconv::f32(K - q) * im));
     const float a = (x0 + 2.f * (1.f - x0) * x1) * lean64::rcp_approx(1.f + (1.f - x1) * sqrtf(fmaxf(1.f - x0, 0.f)));
-    if (!(fabsf(a - 1.f) > 1e-5f) || !(a > 1e-30f && a < 1e30f) || !(x0 < 0.9f)) {
-        const double am = pprod_argmin_exact(K, q, c);
-        return !((am >= 1.) || (am <= 0.));
+    if (fabsf(a - 1.f) > 1e-5f && a > 1e-30f && a < 1e30f && x0 < 0.9f)
+        return a < 1.f;
+    // Float-float argmin (~1e-13 relative here) where float could not decide:
+    // argmin - 1 beyond 1e-10 decides.  Near q = 4 me (1 - x0 < 1e-4, where
+    // 1 - x0 amplifies the error of x0) and for extreme K the IEEE value does.
+    if (x0 < 0.9999f && fpconv::f32(K) < 1e15f) {
+        const FF am = pprod_argmin_ff(K, q, c);
+        const float d = (am.h - 1.f) + am.l;  // am.h - 1 is exact for am.h in [0.5, 2]
+        if (am.h >= 0.5f && am.h <= 2.f && fabsf(d) > 1e-10f)
+            return d < 0.f;
+        if (am.h > 1e-30f && am.h < 0.5f)
+            return true;
+        if (am.h > 2.f && am.h < 1e30f)
+            return false;
     }
-    return a < 1.f;
+    const double am = pprod_argmin_exact(K, q, c);
+    return !((am >= 1.) || (am <= 0.));
 }
 
 __device__ __forceinline__ double pprod_fp64(double K, double q, const noa_dcs_consts &c) {

@@ -24,7 +24,8 @@
  */
 #pragma once
 
-#include "dcs_common.cuh"
+#include "dcs_fp32c.cuh"
+#include "dcs_fp64.cuh"
 
 #include <cuda_bf16.h>
 
@@ -96,10 +97,7 @@ __device__ __forceinline__ bool baseline(double K, double q, const noa_dcs_const
     }
 }
 
-// Inference form of baseline(): the open / closed decision in float with the
-// exact IEEE decision near a bound (the FP64 kernels' float-first checks), and
-// the baseline as a sum of float logs (about 1e-6 absolute, far below the
-// surrogate's 1e-3).  Returns false for a closed pair.
+// Inference forms of baseline().
 // Float pre-check of the reference's first early returns: true only where
 // the pair is certainly closed (margins of 1e-5 relative, far above float
 // rounding); the exact checks decide everything else.
@@ -111,41 +109,39 @@ __device__ __forceinline__ bool surely_closed(double K, double q, const noa_dcs_
     return qf < 0.99999f || qf < 2E-03f * Kf * 0.99999f;
 }
 
+// The open / closed decision as the FP64 kernels take it: float first, the
+// exact IEEE decision near a bound.
 template <int PROC>
-__device__ __forceinline__ bool baseline_fast(double K, double q, const noa_dcs_consts &c, float &base) {
-    using namespace noa_dcs;
+__device__ __forceinline__ bool open_fast(double K, double q, const noa_dcs_consts &c) {
     if (surely_closed<PROC>(K, q, c))
         return false;
+    return PROC == NOA_DCS_PAIR_PRODUCTION ? noa_dcs::pprod_live(K, q, c) : noa_dcs::photo_live(K, q, c);
+}
+
+// The baseline of an open pair as a sum of float logs (about 1e-6 absolute,
+// far below the surrogate's 1e-3).  False where float cannot form it
+// (photonuclear within 1e-4 of its Q2 window closing): the pair then goes to
+// the fallback.
+template <int PROC>
+__device__ __forceinline__ bool baseline_value(double K, double q, const noa_dcs_consts &c, float &base) {
+    using namespace noa_dcs;
     const double mass = c.mass;
     const double E = K + mass;
     const float Ef = fpconv::f32(E), qf = fpconv::f32(q), Emq = fpconv::f32(E - q);
     if (PROC == NOA_DCS_PAIR_PRODUCTION) {
-        if (!pprod_live(K, q, c))
-            return false;
-        // argmin in float (as pprod_live), its log, and the prefactor
-        const float im = fpconv::f32(c.inv_mass);
-        const float x0 = (float)(4. * ME) / qf;
-        const float gamma = 1.f + fpconv::f32(K) * im;
-        const float x1 = 6.f / (gamma * (1.f + fpconv::f32(K - q) * im));
-        const float a = (x0 + 2.f * (1.f - x0) * x1) / (1.f + (1.f - x1) * sqrtf(fmaxf(1.f - x0, 0.f)));
-        // near argmin -> 1, -log(argmin) needs argmin's FP64 value
-        const float tmin = (a > 0.99f || !(x0 < 0.9f)) ? fpconv::f32(d_log(pprod_argmin_exact(K, q, c))) : logf(a);
+        // log(argmin) from the float-float argmin, through log1p near
+        // argmin = 1 (where a.h - 1 is exact)
+        const FF a = pprod_argmin_ff(K, q, c);
+        const float tmin = a.h >= 0.5f ? log1pf((a.h - 1.f) + a.l) : logf(a.h);
         base = logf(fpconv::f32(c.pp_cZ * c.Zd * c.scale_A)) + logf(Emq) - logf(qf) - logf(Ef) +
                logf(fpconv::f32(mass + K)) + logf(-tmin);
         return true;
     } else {
-        if (!photo_live(K, q, c))  // float first, exact near the bounds
-            return false;
         const float y = qf / Ef, omy = Emq / Ef;
         const float Q2min = fpconv::f32(mass * mass) * y * y / omy;
         const float Q2max = (float)(2.0 * PH_M) * fpconv::f32(q - PH_MPI) - (float)(PH_MPI * PH_MPI);
-        if (fabsf(Q2max - Q2min) <= 1e-4f * fmaxf(fabsf(Q2max), fabsf(Q2min)) || !(Q2min > 0.f)) {
-            double a, b;
-            if (!photo_window(K, q, c, a, b))
-                return false;
-        } else if (Q2max < Q2min) {
+        if (!(Q2max - Q2min > 1e-4f * fmaxf(fabsf(Q2max), fabsf(Q2min))) || !(Q2min > 0.f))
             return false;
-        }
         base = logf(fpconv::f32(2.603096E-35 * c.scale_A)) - logf(qf) + logf(omy + 0.5f * y * y) +
                logf(1.f / Q2min - 1.f / Q2max) + logf(fpconv::f32(mass + K));
         return true;

@@ -1,13 +1,14 @@
 /*
- * Learned DCS surrogate, inference (noa_dcs_mlp_infer): three kernels on the
+ * Learned DCS surrogate, inference (noa_dcs_mlp_infer): four kernels on the
  * caller's stream.
  *
  *  1. classify: per pair, the kinematic bounds decided as the FP64 kernels
- *     decide them (closed -> 0), the float baseline of mlp.cuh, the
- *     normalised features and the trust-grid cell.
- *     Pairs inside the trained domain whose cell passed the held-out error
- *     check go to the network list; the others to the fallback list (both in
- *     the model's scratch, appended with warp-aggregated atomics).
+ *     decide them (closed -> 0), the normalised features and the trust-grid
+ *     cell.  Pairs inside the trained domain whose cell passed the held-out
+ *     error check go to the network list; the others to the fallback list
+ *     (both in the model's scratch, appended with warp-aggregated atomics).
+ *     Then netprep: the float baseline of mlp.cuh for each listed pair,
+ *     densely over the list.
  *  2. network (tcgen05): a persistent CTA of four warpgroups evaluates tiles of
  *     128 listed pairs.  Row r of a tile is TMEM lane r.  Layer 1 (4 -> 128)
  *     and the output layer run in FP32 on the CUDA cores; the two 128 x 128
@@ -84,54 +85,135 @@ __device__ __forceinline__ void append(unsigned long long *counter, bool flag, i
     slot = flag ? (int)(base + __popc(m & ((1u << lane) - 1u))) : -1;
 }
 
+// Classify, in tiles of 256 x CL_ITEMS pairs: the list positions come from a
+// block-wide scan and one atomicAdd per list per tile (one per warp, with
+// every warp of the grid on the same two counters, serialised in L2 and
+// took most of this kernel's time).
+constexpr int CL_THREADS = 256, CL_ITEMS = 4;
+
 template <int PROC>
-__global__ void __launch_bounds__(256) classify_kernel(const __grid_constant__ InferParams p) {
+__global__ void __launch_bounds__(CL_THREADS) classify_kernel(const __grid_constant__ InferParams p) {
+    __shared__ int warp_n[CL_THREADS / 32], warp_f[CL_THREADS / 32];
+    __shared__ unsigned long long base_n, base_f;
+    __shared__ float4 s_feat[CL_ITEMS][CL_THREADS];  // the items stay rolled (one copy of the bound checks)
+    __shared__ uint8_t s_seg[CL_ITEMS][CL_THREADS];
     const int64_t n = p.seg_begin[p.n_seg];
-    for (int64_t base = (int64_t)blockIdx.x * blockDim.x; base < n; base += (int64_t)gridDim.x * blockDim.x) {
-        const int64_t i = base + threadIdx.x;
-        bool to_net = false, to_fb = false;
-        int seg = 0;
-        float b = 0.f;
-        float4 f = make_float4(0.f, 0.f, 0.f, 0.f);
-        if (i < n) {
-            while (seg + 1 < p.n_seg && i >= p.seg_begin[seg + 1])
-                seg++;
-            const noa_dcs_consts &c = p.consts[seg];
-            const double K = p.K[i], q = p.q[i];
-            float bf;
-            if (!baseline_fast<PROC>(K, q, c, bf)) {
-                p.out[i] = 0.;
-            } else {
-                const float lk = logf(fpconv::f32(K)), ln = logf(fpconv::f32(q) / fpconv::f32(K + c.mass));
-                const float fk = floorf((lk - p.logk_lo) / p.logk_span * 64.f);
-                const float fn = floorf((ln - p.lognu_lo) / p.lognu_span * 64.f);
-                bool trusted = false;
-                if (fk >= 0.f && fk < 64.f && fn >= 0.f && fn < 64.f && isfinite(bf))
-                    trusted = p.trust[(seg * 64 + (int)fk) * 64 + (int)fn] != 0;
-                if (trusted) {
-                    to_net = true;
-                    b = bf;
-                    f.x = (lk - p.norm.in_shift[0]) * p.norm.in_scale[0];
-                    f.y = (ln - p.norm.in_shift[1]) * p.norm.in_scale[1];
-                    f.z = (p.Zf[seg] * 0.01f - p.norm.in_shift[2]) * p.norm.in_scale[2];
-                    f.w = (p.logA[seg] - p.norm.in_shift[3]) * p.norm.in_scale[3];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    for (int64_t tile = (int64_t)blockIdx.x * CL_THREADS * CL_ITEMS; tile < n;
+         tile += (int64_t)gridDim.x * CL_THREADS * CL_ITEMS) {
+        unsigned net_mask = 0, fb_mask = 0;
+#pragma unroll 1
+        for (int j = 0; j < CL_ITEMS; j++) {
+            const int64_t i = tile + j * CL_THREADS + threadIdx.x;
+            float4 f = make_float4(0.f, 0.f, 0.f, 0.f);
+            int seg = 0;
+            if (i < n) {
+                while (seg + 1 < p.n_seg && i >= p.seg_begin[seg + 1])
+                    seg++;
+                const noa_dcs_consts &c = p.consts[seg];
+                const double K = p.K[i], q = p.q[i];
+                if (!open_fast<PROC>(K, q, c)) {
+                    p.out[i] = 0.;
                 } else {
-                    to_fb = true;
+                    const float lk = logf(fpconv::f32(K)), ln = logf(fpconv::f32(q) / fpconv::f32(K + c.mass));
+                    const float fk = floorf((lk - p.logk_lo) / p.logk_span * 64.f);
+                    const float fn = floorf((ln - p.lognu_lo) / p.lognu_span * 64.f);
+                    bool trusted = false;
+                    if (fk >= 0.f && fk < 64.f && fn >= 0.f && fn < 64.f)
+                        trusted = p.trust[(seg * 64 + (int)fk) * 64 + (int)fn] != 0;
+                    if (trusted) {
+                        net_mask |= 1u << j;
+                        f.x = (lk - p.norm.in_shift[0]) * p.norm.in_scale[0];
+                        f.y = (ln - p.norm.in_shift[1]) * p.norm.in_scale[1];
+                        f.z = (p.Zf[seg] * 0.01f - p.norm.in_shift[2]) * p.norm.in_scale[2];
+                        f.w = (p.logA[seg] - p.norm.in_shift[3]) * p.norm.in_scale[3];
+                    } else {
+                        fb_mask |= 1u << j;
+                    }
                 }
             }
+            s_feat[j][threadIdx.x] = f;
+            s_seg[j][threadIdx.x] = (uint8_t)seg;
         }
-        int s_net, s_fb;
-        append(&p.counters[0], to_net, s_net);
+        // block-wide exclusive scan of the two counts
+        const int cn = __popc(net_mask), cf = __popc(fb_mask);
+        int sn = cn, sf = cf;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int yn = __shfl_up_sync(0xffffffffu, sn, o), yf = __shfl_up_sync(0xffffffffu, sf, o);
+            if (lane >= o) {
+                sn += yn;
+                sf += yf;
+            }
+        }
+        if (lane == 31) {
+            warp_n[warp] = sn;
+            warp_f[warp] = sf;
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            int tn = 0, tf = 0;
+            for (int w = 0; w < CL_THREADS / 32; w++) {
+                const int a = warp_n[w], b = warp_f[w];
+                warp_n[w] = tn;
+                warp_f[w] = tf;
+                tn += a;
+                tf += b;
+            }
+            base_n = tn ? atomicAdd(&p.counters[0], (unsigned long long)tn) : 0ull;
+            base_f = tf ? atomicAdd(&p.counters[1], (unsigned long long)tf) : 0ull;
+        }
+        __syncthreads();
+        unsigned long long pn = base_n + (unsigned long long)(warp_n[warp] + sn - cn);
+        unsigned long long pf = base_f + (unsigned long long)(warp_f[warp] + sf - cf);
+#pragma unroll
+        for (int j = 0; j < CL_ITEMS; j++) {
+            const int32_t i = (int32_t)(tile + j * CL_THREADS + threadIdx.x);
+            if (net_mask & (1u << j)) {
+                p.net_idx[pn] = i;
+                p.net_feat[pn] = s_feat[j][threadIdx.x];
+                p.net_seg[pn] = s_seg[j][threadIdx.x];
+                pn++;
+            }
+            if (fb_mask & (1u << j)) {
+                p.fb_idx[pf] = i;
+                p.fb_seg[pf] = s_seg[j][threadIdx.x];
+                pf++;
+            }
+        }
+        __syncthreads();  // warp_n / warp_f and the bases are rewritten by the next tile
+    }
+}
+
+// Baselines of the network list, computed densely over the list (in the
+// classify kernel only the trusted lanes would need them, and the others
+// would wait).  A pair whose baseline float cannot form moves to the
+// fallback list; its network row is computed but not written (index -1).
+template <int PROC>
+__global__ void __launch_bounds__(256) netprep_kernel(const __grid_constant__ InferParams p) {
+    const unsigned long long cnt = p.counters[0];
+    for (unsigned long long base = (unsigned long long)blockIdx.x * blockDim.x; base < cnt;
+         base += (unsigned long long)gridDim.x * blockDim.x) {
+        const unsigned long long e = base + threadIdx.x;
+        bool to_fb = false;
+        int32_t i = 0;
+        uint8_t sg = 0;
+        if (e < cnt) {
+            i = p.net_idx[e];
+            sg = p.net_seg[e];
+            float bf;
+            if (baseline_value<PROC>(p.K[i], p.q[i], p.consts[sg], bf) && isfinite(bf)) {
+                p.net_base[e] = bf;
+            } else {
+                p.net_idx[e] = -1;
+                to_fb = true;
+            }
+        }
+        int s_fb;
         append(&p.counters[1], to_fb, s_fb);
-        if (to_net) {
-            p.net_idx[s_net] = (int32_t)i;
-            p.net_base[s_net] = b;
-            p.net_feat[s_net] = f;
-            p.net_seg[s_net] = (uint8_t)seg;
-        }
         if (to_fb) {
-            p.fb_idx[s_fb] = (int32_t)i;
-            p.fb_seg[s_fb] = (uint8_t)seg;
+            p.fb_idx[s_fb] = i;
+            p.fb_seg[s_fb] = sg;
         }
     }
 }
@@ -421,9 +503,11 @@ __global__ void __launch_bounds__(NT, 1) network_kernel(const __grid_constant__ 
         fence_before();
         __syncthreads();
         if (quarter == 0 && valid) {
+            const int32_t oi = p.net_idx[e];
             const float yy = y + spart[0][row] + spart[1][row] + spart[2][row] + bo;
             const float r = p.norm.out_shift + yy / p.norm.out_scale;
-            p.out[p.net_idx[e]] = fpconv::f64(expf(p.net_base[e] + r));
+            if (oi >= 0)
+                p.out[oi] = fpconv::f64(expf(p.net_base[e] + r));
         }
     }
     if (s_abort && tid == 0)
@@ -549,11 +633,20 @@ extern "C" int noa_dcs_mlp_infer(noa_dcs_mlp *model, const uint8_t *trust, int n
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     const int64_t blocks = (n + 255) / 256;
     const int cgrid = (int)(blocks < sms * 8 ? blocks : sms * 8);
+    const int64_t ctiles = (n + CL_THREADS * CL_ITEMS - 1) / (CL_THREADS * CL_ITEMS);
+    const int clgrid = (int)(ctiles < sms * 8 ? ctiles : sms * 8);
     if (e == cudaSuccess) {
         if (process == NOA_DCS_PAIR_PRODUCTION)
-            classify_kernel<NOA_DCS_PAIR_PRODUCTION><<<cgrid, 256, 0, s>>>(p);
+            classify_kernel<NOA_DCS_PAIR_PRODUCTION><<<clgrid, CL_THREADS, 0, s>>>(p);
         else
-            classify_kernel<NOA_DCS_PHOTONUCLEAR><<<cgrid, 256, 0, s>>>(p);
+            classify_kernel<NOA_DCS_PHOTONUCLEAR><<<clgrid, CL_THREADS, 0, s>>>(p);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) {
+        if (process == NOA_DCS_PAIR_PRODUCTION)
+            netprep_kernel<NOA_DCS_PAIR_PRODUCTION><<<cgrid, 256, 0, s>>>(p);
+        else
+            netprep_kernel<NOA_DCS_PHOTONUCLEAR><<<cgrid, 256, 0, s>>>(p);
         e = cudaGetLastError();
     }
     if (e == cudaSuccess) {
