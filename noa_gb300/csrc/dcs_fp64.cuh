@@ -86,6 +86,32 @@ __device__ __forceinline__ double brems_fp64(double K, double q, const noa_dcs_c
 }
 
 // ---------------------------------------------------------------- pair production
+// The rare part of pprod_live, out of line so that the kernels that inline
+// pprod_live once per item keep one copy of it: the float-float argmin
+// (~1e-13 relative here), whose distance from 1 decides beyond 1e-10, and
+// the IEEE argmin near q = 4 me (1 - x0 < 1e-4, where 1 - x0 amplifies the
+// error of x0), for extreme K, or within 1e-10.  Scalars only (a reference
+// to the constants would copy them to local memory).
+static __device__ __noinline__ bool pprod_live_tail(double K, double q, double mass, float inv_mass_h, float inv_mass_l,
+                                             float x0) {
+    noa_dcs_consts c;
+    c.mass = mass;
+    c.inv_mass_h = inv_mass_h;
+    c.inv_mass_l = inv_mass_l;
+    if (x0 < 0.9999f && fpconv::f32(K) < 1e15f) {
+        const FF am = pprod_argmin_ff(K, q, c);
+        const float d = (am.h - 1.f) + am.l;  // am.h - 1 is exact for am.h in [0.5, 2]
+        if (am.h >= 0.5f && am.h <= 2.f && fabsf(d) > 1e-10f)
+            return d < 0.f;
+        if (am.h > 1e-30f && am.h < 0.5f)
+            return true;
+        if (am.h > 2.f && am.h < 1e30f)
+            return false;
+    }
+    const double am = pprod_argmin_exact(K, q, c);
+    return !((am >= 1.) || (am <= 0.));
+}
+
 __device__ __forceinline__ bool pprod_live(double K, double q, const noa_dcs_consts &c) {
     if (q <= 4. * ME)
         return false;
@@ -100,21 +126,7 @@ __device__ __forceinline__ bool pprod_live(double K, double q, const noa_dcs_con
     const float a = (x0 + 2.f * (1.f - x0) * x1) * lean64::rcp_approx(1.f + (1.f - x1) * sqrtf(fmaxf(1.f - x0, 0.f)));
     if (fabsf(a - 1.f) > 1e-5f && a > 1e-30f && a < 1e30f && x0 < 0.9f)
         return a < 1.f;
-    // Float-float argmin (~1e-13 relative here) where float could not decide:
-    // argmin - 1 beyond 1e-10 decides.  Near q = 4 me (1 - x0 < 1e-4, where
-    // 1 - x0 amplifies the error of x0) and for extreme K the IEEE value does.
-    if (x0 < 0.9999f && fpconv::f32(K) < 1e15f) {
-        const FF am = pprod_argmin_ff(K, q, c);
-        const float d = (am.h - 1.f) + am.l;  // am.h - 1 is exact for am.h in [0.5, 2]
-        if (am.h >= 0.5f && am.h <= 2.f && fabsf(d) > 1e-10f)
-            return d < 0.f;
-        if (am.h > 1e-30f && am.h < 0.5f)
-            return true;
-        if (am.h > 2.f && am.h < 1e30f)
-            return false;
-    }
-    const double am = pprod_argmin_exact(K, q, c);
-    return !((am >= 1.) || (am <= 0.));
+    return pprod_live_tail(K, q, c.mass, c.inv_mass_h, c.inv_mass_l, x0);
 }
 
 __device__ __forceinline__ double pprod_fp64(double K, double q, const noa_dcs_consts &c) {

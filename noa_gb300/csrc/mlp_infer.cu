@@ -388,7 +388,8 @@ __global__ void __launch_bounds__(NT, 1) network_kernel(const __grid_constant__ 
     unsigned char *sm = smem_raw + ((1024 - (smem_u32(smem_raw) & 1023)) & 1023);
     unsigned char *W2h = sm, *W2l = sm + MAT, *W3h = sm + 2 * MAT, *W3l = sm + 3 * MAT;
     unsigned char *Ahi = sm + 4 * MAT, *Alo = sm + 5 * MAT;
-    __shared__ float sW1[H * IN], sb1[H], sb2[H], sb3[H], sWo[H];
+    __shared__ __align__(16) float sW1[H * IN];
+    __shared__ float sb1[H], sb2[H], sb3[H], sWo[H];
     __shared__ float spart[3][TILE];
     __shared__ uint32_t tmem_slot;
     __shared__ __align__(8) unsigned long long mbar;
@@ -437,25 +438,40 @@ __global__ void __launch_bounds__(NT, 1) network_kernel(const __grid_constant__ 
     uint32_t phase = 0;
 
     const long long tiles = (long long)((cnt + TILE - 1) / TILE);
+    // the features of a row (and, for the output threads, its index and
+    // baseline) are loaded one tile ahead, so their latency overlaps the MMAs
+    auto load_feat = [&](long long t) {
+        const long long e = t * TILE + row;
+        return (t < tiles && e < (long long)cnt) ? p.net_feat[e] : make_float4(0.f, 0.f, 0.f, 0.f);
+    };
+    float4 f = load_feat(blockIdx.x);
     for (long long t = blockIdx.x; t < tiles; t += gridDim.x) {
         const long long e = t * TILE + row;
         const bool valid = e < (long long)cnt;
-        float4 f = valid ? p.net_feat[e] : make_float4(0.f, 0.f, 0.f, 0.f);
+        int32_t oi = -1;
+        float obase = 0.f;
+        if (quarter == 0 && valid) {
+            oi = p.net_idx[e];
+            obase = p.net_base[e];
+        }
+        const float4 f_next = load_feat(t + gridDim.x);
         // layer 1 (FP32): this thread's 32 hidden units of its row
         for (int k0 = quarter * 32; k0 < quarter * 32 + 32; k0 += 8) {
             float h[8];
 #pragma unroll
             for (int j = 0; j < 8; j++) {
                 const int u = k0 + j;
+                const float4 w = reinterpret_cast<const float4 *>(sW1)[u];
                 float z = sb1[u];
-                z = fmaf(sW1[u * 4 + 0], f.x, z);
-                z = fmaf(sW1[u * 4 + 1], f.y, z);
-                z = fmaf(sW1[u * 4 + 2], f.z, z);
-                z = fmaf(sW1[u * 4 + 3], f.w, z);
+                z = fmaf(w.x, f.x, z);
+                z = fmaf(w.y, f.y, z);
+                z = fmaf(w.z, f.z, z);
+                z = fmaf(w.w, f.w, z);
                 h[j] = silu(z);
             }
             put8(Ahi, Alo, row, k0, h);
         }
+        f = f_next;
         // layers 2 and 3 on the tensor cores
         float y = 0.f;
 #pragma unroll 1
@@ -503,11 +519,10 @@ __global__ void __launch_bounds__(NT, 1) network_kernel(const __grid_constant__ 
         fence_before();
         __syncthreads();
         if (quarter == 0 && valid) {
-            const int32_t oi = p.net_idx[e];
             const float yy = y + spart[0][row] + spart[1][row] + spart[2][row] + bo;
             const float r = p.norm.out_shift + yy / p.norm.out_scale;
             if (oi >= 0)
-                p.out[oi] = fpconv::f64(expf(p.net_base[e] + r));
+                p.out[oi] = fpconv::f64(expf(obase + r));
         }
     }
     if (s_abort && tid == 0)
