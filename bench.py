@@ -15,9 +15,11 @@ nu ~ log-uniform[1e-7, 1], q = nu K (noa_gb300.workload, seed 987654).
 events on the launching stream; K and q are 160 MB, above the 129 MB L2, so
 no flush is needed between steps).  `e2e` is the same metric through the C
 ABI's host-buffer entry point (noa_dcs_vmap_host) from pinned host memory,
-copies included.  `--impl reference` times the reference algorithm on the
-host cores instead (the CPU oracle, an operation-for-operation restatement of
-src/noa/pms/dcs.hh, OpenMP over all cores like dcs::pvmap).
+host-device traffic included: the kernels read K and q and write the results
+in the page-locked host buffers over NVLink-C2C.  `--impl reference` times
+the reference algorithm on the host cores instead (the CPU oracle, an
+operation-for-operation restatement of src/noa/pms/dcs.hh, OpenMP over all
+cores like dcs::pvmap).
 """
 import argparse
 import json
@@ -621,7 +623,7 @@ def run_ours(args):
             parity[name] = {"mean_rel": float(rel.mean()), "max_rel": float(rel.max()),
                             "zero_pattern_equal": bool(np.array_equal(got == 0, ref == 0))}
 
-    # e2e: host buffers in pinned memory, through noa_dcs_vmap_host, copies timed.
+    # e2e: host buffers in pinned memory, through noa_dcs_vmap_host, host-device traffic timed.
     e2e = None
     if not args.no_e2e:
         hk = torch.from_numpy(K).pin_memory()
@@ -643,7 +645,7 @@ def run_ours(args):
         t_e2e = reduce_max(t_e2e, world, dev)
         e2e = {"value": world * 4 * n * e2e_steps / t_e2e, "unit": "evals/s",
                "h2d_bytes_per_step": 4 * 2 * 8 * n, "d2h_bytes_per_step": 4 * 8 * n, "steps": e2e_steps,
-               "path": "noa_dcs_vmap_host (pinned host buffers, chunked copy/compute pipeline)"}
+               "path": "noa_dcs_vmap_host (pinned host buffers read and written in place by the kernels over NVLink-C2C)"}
         # correctness of the timed e2e results against the device path
         for p in range(4):
             if not torch.equal(hout[p], outs[p].cpu()):

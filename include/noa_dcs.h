@@ -140,13 +140,14 @@ int noa_dcs_cuda_hard_scattering(double *mu0, double *lb_h, const double *G, con
 int noa_dcs_cuda_vmap_fp32c(int process, double *result, const double *K, const double *q, int64_t n,
                             const noa_dcs_element *element, double mass, float tolerance, void *stream);
 
-/* Host-buffer form: K, q and result are HOST buffers (pinned memory gives
- * copy/compute overlap; pageable memory works but serialises the copies).
- * The call stages the data through device buffers owned by the library,
- * pipelining host-to-device copies, kernels and device-to-host copies in
- * chunks on its own streams, and returns when result is complete.  This is the
- * GPU counterpart of calling dcs::vmap / dcs::pvmap on CPU tensors
- * (dcs.hh:35-75). */
+/* Host-buffer form: K, q and result are HOST buffers.  When all three are
+ * page-locked (cudaHostAlloc / cudaHostRegister, e.g. torch pin_memory), the
+ * kernels read and write them in place over the CPU-GPU link, with no
+ * staging.  Otherwise the call stages the data through device buffers owned
+ * by the library, pipelining host-to-device copies, kernels and
+ * device-to-host copies in chunks on its own streams.  Either way it returns
+ * when result is complete.  This is the GPU counterpart of calling dcs::vmap /
+ * dcs::pvmap on CPU tensors (dcs.hh:35-75). */
 int noa_dcs_vmap_host(int process, int precision, double *result, const double *K, const double *q, int64_t n,
                       const noa_dcs_element *element, double mass);
 

@@ -125,6 +125,24 @@ int staging_acquire(Staging &s) {
     return NOA_DCS_SUCCESS;
 }
 
+// The device address of a page-locked host buffer of n doubles that the
+// kernels can read and write in place (over NVLink-C2C on Grace-Blackwell),
+// or nullptr: pageable memory, or a mapping that is not the identity of
+// unified addressing.  The first and the last element must both lie in
+// page-locked memory.
+const double *device_view(const double *p, int64_t n) {
+    for (const double *x : {p, p + (n - 1)}) {
+        cudaPointerAttributes a;
+        if (cudaPointerGetAttributes(&a, x) != cudaSuccess) {
+            cudaGetLastError();
+            return nullptr;
+        }
+        if (a.type != cudaMemoryTypeHost || a.devicePointer != (const void *)x)
+            return nullptr;
+    }
+    return p;
+}
+
 } // namespace
 
 static int vmap_checked(int process, int precision, double *result, const double *K, const double *q, int64_t n,
@@ -358,6 +376,16 @@ int noa_dcs_vmap_host(int process, int precision, double *result, const double *
     std::lock_guard<std::mutex> lock(s.mu);
     if ((st = staging_acquire(s)))
         return st;
+    // page-locked buffers: the kernels read K and q and write the result in
+    // place, with no staging copies (the link carries the same 24 bytes per
+    // pair, overlapped with the compute by the kernels' own loads and stores)
+    if (device_view(K, n) && device_view(q, n) && device_view(result, n)) {
+        if ((st = launch(process, precision, result, K, q, n, &c, s.st[0])))
+            return st;
+        if ((e = cudaStreamSynchronize(s.st[0])) != cudaSuccess)
+            return cuda_fail(e, "cudaStreamSynchronize");
+        return NOA_DCS_SUCCESS;
+    }
     for (int64_t off = 0, chunk = 0; off < n; off += kChunk, chunk++) {
         const int slot = (int)(chunk % kSlots);
         const int64_t m = (n - off) < kChunk ? (n - off) : kChunk;
