@@ -73,7 +73,9 @@ def map(process, kinetic_energies, recoil_energies, element=STANDARD_ROCK, mass=
 def vmap_host(process, result, kinetic_energies, recoil_energies, element=STANDARD_ROCK, mass=MUON_MASS,
               precision="fp64"):
     """Host-buffer path (noa_dcs_vmap_host): CPU float64 tensors in and out,
-    staged through the GPU; returns when result is filled."""
+    computed on the GPU; returns when result is filled.  Pinned tensors
+    (pin_memory) are read and written in place by the kernels; pageable ones
+    are staged through device buffers."""
     lib = _lib.load()
     for t, name in ((result, "result"), (kinetic_energies, "kinetic_energies"),
                     (recoil_energies, "recoil_energies")):

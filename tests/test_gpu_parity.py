@@ -128,6 +128,26 @@ def test_host_buffer_path(cuda_device, process, pinned):
     assert same_bits(out.numpy(), dev)
 
 
+@pytest.mark.parametrize("layout", ["pageable_result", "offsets_in_pinned"])
+def test_host_buffer_path_mixed(cuda_device, layout):
+    """Page-locked buffers are worked on in place only when all three are;
+    pinned inputs with a pageable result go through the staging pipeline, and
+    slices that start inside a pinned allocation are used in place."""
+    n = (1 << 21) + 777
+    K, q = kinetic_recoil(n + 64, offset=9 << 20)
+    tk, tq = torch.from_numpy(K).pin_memory(), torch.from_numpy(q).pin_memory()
+    if layout == "pageable_result":
+        a, b, out = tk[:n], tq[:n], torch.empty(n, dtype=torch.float64)
+        Ks, qs = K[:n], q[:n]
+    else:
+        buf = torch.empty(n + 64, dtype=torch.float64).pin_memory()
+        a, b, out = tk[64:], tq[64:], buf[64:]
+        Ks, qs = K[64:], q[64:]
+    for process in range(4):
+        dcs.vmap_host(process, out, a, b)
+        assert same_bits(out.numpy(), gpu_dcs(process, Ks, qs))
+
+
 @pytest.mark.parametrize("process", range(4), ids=PROCESSES)
 def test_runs_on_the_current_stream(cuda_device, process):
     K, q = kinetic_recoil(300000, offset=4242)
