@@ -9,25 +9,29 @@
  *     (both in the model's scratch, appended with warp-aggregated atomics).
  *     Then netprep: the float baseline of mlp.cuh for each listed pair,
  *     densely over the list.
- *  2. network (tcgen05): a persistent CTA of four warpgroups evaluates tiles of
- *     128 listed pairs.  Row r of a tile is TMEM lane r.  Layer 1 (4 -> 128)
- *     and the output layer run in FP32 on the CUDA cores; the two 128 x 128
- *     layers run on the 5th-generation tensor cores: the activations are
- *     written to shared memory as BF16 hi / lo in the canonical no-swizzle
- *     K-major layout, W2 and W3 (hi / lo, resident in shared memory for the
- *     whole launch) are the B operands, and one thread issues
- *     tcgen05.mma.cta_group::1.kind::f16 (M = N = 128, K = 16) for the three
- *     products A_hi W_hi + A_lo W_hi + A_hi W_lo, accumulating in FP32 in TMEM.
- *     tcgen05.commit signals an mbarrier; the epilogue reads the accumulator
- *     with tcgen05.ld (warpgroup g reads columns 32g .. 32g+31 of the same
- *     128 lanes), adds the bias and applies SiLU.
+ *  2. network (tcgen05): a persistent CTA of four warpgroups keeps two tiles
+ *     of 128 listed pairs in flight, two warpgroups each, so that the tensor
+ *     core works on one tile while the CUDA cores run the other's SiLU
+ *     epilogue.  Row r of a tile is TMEM lane r; a thread owns one row and 64
+ *     of its 128 hidden units.  Layer 1 (4 -> 128) and the output layer run in
+ *     FP32 on the CUDA cores; the two 128 x 128 layers run on the
+ *     5th-generation tensor cores.  The activations are written to TMEM
+ *     (tcgen05.st) as BF16 hi / lo, two per 32-bit column, and are the A
+ *     operand of tcgen05.mma.cta_group::1.kind::f16 (M = N = 128, K = 16);
+ *     W2 and W3 (hi / lo, resident in shared memory in the canonical
+ *     no-swizzle K-major layout for the whole launch) are the B operands.
+ *     One thread per tile issues the three products A_hi W_hi + A_lo W_hi +
+ *     A_hi W_lo, accumulating in FP32 in TMEM, and commits to the tile's
+ *     mbarrier; the epilogue reads the accumulator with tcgen05.ld, adds the
+ *     bias and applies SiLU.  TMEM per tile: accumulator 128 columns, A hi 64,
+ *     A lo 64 (512 for the two).
  *     DCS = exp(baseline + residual), in float (1e-6 relative).
  *  3. fallback: the FP32C evaluation (dcs_fp32c.cuh) of the fallback list,
  *     with FP64 (dcs_fp64.cuh) for pairs above its tolerance.
  *
  * Every mbarrier wait is bounded; on expiry the kernel records
- * NOA_DCS_ERROR_TIMEOUT in the model's status word, finishes its in-flight
- * MMAs, frees its TMEM and returns.
+ * NOA_DCS_ERROR_TIMEOUT in the model's status word, gives the MMAs still in
+ * flight one more bounded wait, frees its TMEM and returns.
  */
 #include "dcs_fp32c.cuh"
 #include "dcs_fp64.cuh"
@@ -45,9 +49,11 @@ using namespace noa_mlp;
 namespace {
 
 constexpr int NT = 512;                   // threads of the network kernel: 4 warpgroups
+constexpr int SLOTS = 2;                  // tiles in flight per CTA, two warpgroups each
 constexpr int TILE = 128;                 // rows (pairs) per tile = TMEM lanes
+constexpr int TMEM_COLS = 512;            // per slot: accumulator 128 + A hi 64 + A lo 64 columns
 constexpr int MAT = H * H * 2;            // bytes of one 128 x 128 BF16 operand
-constexpr int SMEM_NET = 6 * MAT + 1024;  // W2 hi/lo, W3 hi/lo, A hi/lo, alignment slack
+constexpr int SMEM_NET = 4 * MAT + 1024;  // W2 hi/lo, W3 hi/lo, alignment slack
 constexpr int MAX_EL = 16;
 constexpr long long SPIN_LIMIT = 1LL << 26;
 
@@ -302,13 +308,6 @@ __device__ __forceinline__ uint64_t make_desc(uint32_t saddr) {
 constexpr uint32_t IDESC = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(128 >> 3) << 17) |
                            ((uint32_t)(128 >> 4) << 24);
 
-__device__ __forceinline__ void mma_f16(uint32_t d_tmem, uint64_t a, uint64_t b, uint32_t accumulate) {
-    asm volatile("{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
-                 "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}"
-                 :
-                 : "r"(d_tmem), "l"(a), "l"(b), "r"(IDESC), "r"(accumulate));
-}
-
 __device__ __forceinline__ void mma_commit(uint32_t mbar) {
     asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(mbar)
                  : "memory");
@@ -350,34 +349,58 @@ __device__ __forceinline__ void fence_before() { asm volatile("tcgen05.fence::be
 __device__ __forceinline__ void fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
 __device__ __forceinline__ void fence_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
 
-// Writes 8 consecutive activations (k .. k+7 of row r) as BF16 hi / lo.
-__device__ __forceinline__ void put8(unsigned char *Ahi, unsigned char *Alo, int r, int k, const float (&h)[8]) {
-    __nv_bfloat162 hi[4], lo[4];
-#pragma unroll
-    for (int i = 0; i < 4; i++) {
-        const __nv_bfloat16 a = __float2bfloat16_rn(h[2 * i]), b = __float2bfloat16_rn(h[2 * i + 1]);
-        hi[i] = __halves2bfloat162(a, b);
-        lo[i] = __halves2bfloat162(__float2bfloat16_rn(h[2 * i] - __bfloat162float(a)),
-                                   __float2bfloat16_rn(h[2 * i + 1] - __bfloat162float(b)));
-    }
-    const uint32_t o = canon_off(r, k);
-    *reinterpret_cast<uint4 *>(Ahi + o) = *reinterpret_cast<uint4 *>(hi);
-    *reinterpret_cast<uint4 *>(Alo + o) = *reinterpret_cast<uint4 *>(lo);
+// Stores 16 consecutive 32-bit TMEM columns of this warp's 32 lanes.
+__device__ __forceinline__ void tmem_st16(uint32_t taddr, const uint32_t (&r)[16]) {
+    asm volatile("tcgen05.st.sync.aligned.32x32b.x16.b32 [%0], "
+                 "{%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16};"
+                 :
+                 : "r"(taddr), "r"(r[0]), "r"(r[1]), "r"(r[2]), "r"(r[3]), "r"(r[4]), "r"(r[5]), "r"(r[6]),
+                   "r"(r[7]), "r"(r[8]), "r"(r[9]), "r"(r[10]), "r"(r[11]), "r"(r[12]), "r"(r[13]), "r"(r[14]),
+                   "r"(r[15])
+                 : "memory");
 }
 
-// Issues the 8 K-steps x 3 products of one 128 x 128 layer into TMEM column
-// offset dcol, and commits to the mbarrier.  One thread.
-__device__ __forceinline__ void issue_layer(uint32_t tmem, uint32_t dcol, uint32_t a_hi, uint32_t a_lo,
-                                            uint32_t w_hi, uint32_t w_lo, uint32_t mbar) {
+// MMA with the A operand in TMEM (M = 128 lanes, two BF16 per 32-bit column)
+// and B from shared memory.
+__device__ __forceinline__ void mma_f16_ts(uint32_t d_tmem, uint32_t a_tmem, uint64_t b, uint32_t accumulate) {
+    asm volatile("{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+                 "tcgen05.mma.cta_group::1.kind::f16 [%0], [%1], %2, %3, p;\n\t}"
+                 :
+                 : "r"(d_tmem), "r"(a_tmem), "l"(b), "r"(IDESC), "r"(accumulate));
+}
+
+// Packs 32 activations (consecutive hidden units, even unit in the low half)
+// as BF16 hi / lo pairs: 16 + 16 32-bit TMEM columns.
+__device__ __forceinline__ void pack32(const float (&h)[32], uint32_t (&hi)[16], uint32_t (&lo)[16]) {
+#pragma unroll
+    for (int i = 0; i < 16; i++) {
+        const __nv_bfloat16 a = __float2bfloat16_rn(h[2 * i]), b = __float2bfloat16_rn(h[2 * i + 1]);
+        const __nv_bfloat162 ph = __halves2bfloat162(a, b);
+        const __nv_bfloat162 pl = __halves2bfloat162(__float2bfloat16_rn(h[2 * i] - __bfloat162float(a)),
+                                                     __float2bfloat16_rn(h[2 * i + 1] - __bfloat162float(b)));
+        hi[i] = *reinterpret_cast<const uint32_t *>(&ph);
+        lo[i] = *reinterpret_cast<const uint32_t *>(&pl);
+    }
+}
+
+// Issues the 8 K-steps x 3 products of one 128 x 128 layer, A (hi / lo) from
+// TMEM, and commits to the mbarrier.  One thread.
+__device__ __forceinline__ void issue_layer_ts(uint32_t acc, uint32_t a_hi, uint32_t a_lo, uint32_t w_hi,
+                                               uint32_t w_lo, uint32_t mbar) {
     fence_after();
 #pragma unroll
     for (int ks = 0; ks < 8; ks++) {
-        const uint32_t o = ks * 256;  // two core matrices along K per step
-        mma_f16(tmem + dcol, make_desc(a_hi + o), make_desc(w_hi + o), ks > 0);
-        mma_f16(tmem + dcol, make_desc(a_lo + o), make_desc(w_hi + o), 1);
-        mma_f16(tmem + dcol, make_desc(a_hi + o), make_desc(w_lo + o), 1);
+        const uint32_t o = ks * 256;  // B: two core matrices along K per step
+        const uint32_t c = ks * 8;    // A: 16 BF16 = 8 TMEM columns per step
+        mma_f16_ts(acc, a_hi + c, make_desc(w_hi + o), ks > 0);
+        mma_f16_ts(acc, a_lo + c, make_desc(w_hi + o), 1);
+        mma_f16_ts(acc, a_hi + c, make_desc(w_lo + o), 1);
     }
     mma_commit(mbar);
+}
+
+__device__ __forceinline__ void slot_sync(int slot) {
+    asm volatile("bar.sync %0, %1;" ::"r"(1 + slot), "r"(NT / SLOTS) : "memory");
 }
 
 template <int PROC>
@@ -387,16 +410,18 @@ __global__ void __launch_bounds__(NT, 1) network_kernel(const __grid_constant__ 
     // 1024-byte aligned operand area
     unsigned char *sm = smem_raw + ((1024 - (smem_u32(smem_raw) & 1023)) & 1023);
     unsigned char *W2h = sm, *W2l = sm + MAT, *W3h = sm + 2 * MAT, *W3l = sm + 3 * MAT;
-    unsigned char *Ahi = sm + 4 * MAT, *Alo = sm + 5 * MAT;
     __shared__ __align__(16) float sW1[H * IN];
     __shared__ float sb1[H], sb2[H], sb3[H], sWo[H];
-    __shared__ float spart[3][TILE];
+    __shared__ float spart[SLOTS][TILE];
     __shared__ uint32_t tmem_slot;
-    __shared__ __align__(8) unsigned long long mbar;
-    __shared__ int s_abort;
+    __shared__ __align__(8) unsigned long long mbar[SLOTS];
+    __shared__ int s_abort[SLOTS];
 
-    const int tid = threadIdx.x, warp = tid >> 5;
-    const int row = tid & 127, quarter = tid >> 7;  // row = TMEM lane, quarter = column block of 32
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    // two tiles in flight: slot s = warpgroups 2s, 2s+1; a thread owns row
+    // `row` (its TMEM lane) and the 64 hidden units [64 half, 64 half + 64)
+    const int slot = warp / 8, wis = warp % 8, half = wis / 4;
+    const int row = (warp % 4) * 32 + lane;
     const unsigned long long cnt = p.counters[0];
 
     // weights to shared memory (canonical layout): 8 consecutive k of a row are 16 contiguous bytes
@@ -419,91 +444,102 @@ __global__ void __launch_bounds__(NT, 1) network_kernel(const __grid_constant__ 
     }
     const float bo = P[OFF_BO];
     if (warp == 0) {
-        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 256;" ::"r"(smem_u32(&tmem_slot)));
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tmem_slot)),
+                     "r"(TMEM_COLS));
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
     }
-    if (tid == 0) {
-        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&mbar)));
-        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-        s_abort = 0;
+    if (tid < SLOTS) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&mbar[tid])));
+        s_abort[tid] = 0;
     }
+    if (tid == 0)
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     fence_async_smem();
     fence_before();
     __syncthreads();
     fence_after();
-    const uint32_t tmem = tmem_slot;
-    const uint32_t mb = smem_u32(&mbar);
-    const uint32_t a_hi = smem_u32(Ahi), a_lo = smem_u32(Alo);
-    const uint32_t lane_base = (uint32_t)((warp & 3) * 32) << 16;  // this warp's TMEM lane quarter
+    // TMEM columns of this slot: accumulator [0, 128), A hi [128, 192), A lo [192, 256)
+    const uint32_t tbase = tmem_slot + (uint32_t)(slot * 256);
+    const uint32_t acc = tbase, a_hi = tbase + 128, a_lo = tbase + 192;
+    const uint32_t lane_base = (uint32_t)((warp % 4) * 32) << 16;  // this warp's TMEM lane quarter
+    const uint32_t mb = smem_u32(&mbar[slot]);
+    const bool issuer = wis == 0 && lane == 0;
     uint32_t phase = 0;
+    bool pending = false;  // an MMA batch of this slot not yet waited for
 
     const long long tiles = (long long)((cnt + TILE - 1) / TILE);
-    // the features of a row (and, for the output threads, its index and
-    // baseline) are loaded one tile ahead, so their latency overlaps the MMAs
+    const long long stride = (long long)gridDim.x * SLOTS;
     auto load_feat = [&](long long t) {
         const long long e = t * TILE + row;
         return (t < tiles && e < (long long)cnt) ? p.net_feat[e] : make_float4(0.f, 0.f, 0.f, 0.f);
     };
-    float4 f = load_feat(blockIdx.x);
-    for (long long t = blockIdx.x; t < tiles; t += gridDim.x) {
+    float4 f = load_feat((long long)blockIdx.x * SLOTS + slot);
+    for (long long t = (long long)blockIdx.x * SLOTS + slot; t < tiles; t += stride) {
         const long long e = t * TILE + row;
         const bool valid = e < (long long)cnt;
         int32_t oi = -1;
         float obase = 0.f;
-        if (quarter == 0 && valid) {
+        if (half == 0 && valid) {
             oi = p.net_idx[e];
             obase = p.net_base[e];
         }
-        const float4 f_next = load_feat(t + gridDim.x);
-        // layer 1 (FP32): this thread's 32 hidden units of its row
-        for (int k0 = quarter * 32; k0 < quarter * 32 + 32; k0 += 8) {
-            float h[8];
+        const float4 f_next = load_feat(t + stride);
+        // layer 1 (FP32): 64 hidden units of this row, written to TMEM as A
+#pragma unroll 1
+        for (int g = 0; g < 2; g++) {
+            const int k0 = half * 64 + g * 32;
+            float h[32];
 #pragma unroll
-            for (int j = 0; j < 8; j++) {
-                const int u = k0 + j;
-                const float4 w = reinterpret_cast<const float4 *>(sW1)[u];
-                float z = sb1[u];
+            for (int j = 0; j < 32; j++) {
+                const float4 w = reinterpret_cast<const float4 *>(sW1)[k0 + j];
+                float z = sb1[k0 + j];
                 z = fmaf(w.x, f.x, z);
                 z = fmaf(w.y, f.y, z);
                 z = fmaf(w.z, f.z, z);
                 z = fmaf(w.w, f.w, z);
                 h[j] = silu(z);
             }
-            put8(Ahi, Alo, row, k0, h);
+            uint32_t rh[16], rl[16];
+            pack32(h, rh, rl);
+            tmem_st16(a_hi + lane_base + (uint32_t)(k0 / 2), rh);
+            tmem_st16(a_lo + lane_base + (uint32_t)(k0 / 2), rl);
         }
         f = f_next;
-        // layers 2 and 3 on the tensor cores
+        // layers 2 and 3 on the tensor cores; the other slot's tile uses the
+        // CUDA cores meanwhile
         float y = 0.f;
 #pragma unroll 1
         for (int layer = 0; layer < 2; layer++) {
-            fence_async_smem();
+            asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
             fence_before();
-            __syncthreads();
-            if (tid == 0)
-                issue_layer(tmem, layer * 128, a_hi, a_lo, smem_u32(layer ? W3h : W2h), smem_u32(layer ? W3l : W2l),
-                            mb);
+            slot_sync(slot);
+            if (issuer)
+                issue_layer_ts(acc, a_hi, a_lo, smem_u32(layer ? W3h : W2h), smem_u32(layer ? W3l : W2l), mb);
+            pending = true;
             const bool ok = mbar_wait(mb, phase);
-            phase ^= 1u;
             if (!ok)
-                s_abort = 1;
+                s_abort[slot] = 1;
             fence_after();
-            __syncthreads();
-            if (s_abort)
+            slot_sync(slot);
+            if (s_abort[slot])
                 break;
+            phase ^= 1u;
+            pending = false;
             const float *bias = layer ? sb3 : sb2;
-            {
-                const int c0 = quarter * 32;
+#pragma unroll 1
+            for (int g = 0; g < 2; g++) {
+                const int c0 = half * 64 + g * 32;
                 float v[32];
-                tmem_ld32(tmem + lane_base + layer * 128 + c0, v);
+                tmem_ld32(acc + lane_base + (uint32_t)c0, v);
                 if (layer == 0) {
+                    float h[32];
 #pragma unroll
-                    for (int g = 0; g < 4; g++) {
-                        float h[8];
-#pragma unroll
-                        for (int j = 0; j < 8; j++)
-                            h[j] = silu(v[g * 8 + j] + bias[c0 + g * 8 + j]);
-                        put8(Ahi, Alo, row, c0 + g * 8, h);
-                    }
+                    for (int j = 0; j < 32; j++)
+                        h[j] = silu(v[j] + bias[c0 + j]);
+                    uint32_t rh[16], rl[16];
+                    pack32(h, rh, rl);
+                    tmem_st16(a_hi + lane_base + (uint32_t)(c0 / 2), rh);
+                    tmem_st16(a_lo + lane_base + (uint32_t)(c0 / 2), rl);
                 } else {
 #pragma unroll
                     for (int j = 0; j < 32; j++)
@@ -511,27 +547,30 @@ __global__ void __launch_bounds__(NT, 1) network_kernel(const __grid_constant__ 
                 }
             }
         }
-        if (s_abort)
+        if (s_abort[slot])
             break;
-        // output: sum the four column blocks, DCS = exp(baseline + residual)
-        if (quarter > 0)
-            spart[quarter - 1][row] = y;
-        fence_before();
-        __syncthreads();
-        if (quarter == 0 && valid) {
-            const float yy = y + spart[0][row] + spart[1][row] + spart[2][row] + bo;
+        // output: sum the two column halves, DCS = exp(baseline + residual)
+        if (half == 1)
+            spart[slot][row] = y;
+        slot_sync(slot);
+        if (half == 0 && valid) {
+            const float yy = y + spart[slot][row] + bo;
             const float r = p.norm.out_shift + yy / p.norm.out_scale;
             if (oi >= 0)
                 p.out[oi] = fpconv::f64(expf(obase + r));
         }
     }
-    if (s_abort && tid == 0)
+    // after an expired wait, give the slot's MMAs in flight one more bounded
+    // wait before the TMEM they write is freed
+    if (pending && s_abort[slot])
+        mbar_wait(mb, phase);
+    if (tid < SLOTS && s_abort[tid])
         atomicMax(&p.counters[2], (unsigned long long)NOA_DCS_ERROR_TIMEOUT);
     fence_before();
     __syncthreads();
     fence_after();
     if (warp == 0)
-        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 256;" ::"r"(tmem));
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem_slot), "r"(TMEM_COLS));
 }
 
 } // namespace
