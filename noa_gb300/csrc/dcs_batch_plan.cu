@@ -48,12 +48,14 @@ int bfail(int st, const char *msg, cudaError_t e = cudaSuccess) {
     return st;
 }
 
-size_t smem_bytes(int threads, int items) {
-    return threads == 128 ? noa_dcs::BatchSmem<128>::bytes(items) : noa_dcs::BatchSmem<256>::bytes(items);
+size_t smem_bytes(const noa_dcs_batch_plan *p, int threads, int items) {
+    const bool third = noa_dcs::batch_third_queue(p->process, p->precision);
+    return threads == 128 ? noa_dcs::BatchSmem<128>::bytes(items, third)
+                          : noa_dcs::BatchSmem<256>::bytes(items, third);
 }
 
 int occupancy(const noa_dcs_batch_plan *p, int threads, int items) {
-    const size_t smem = smem_bytes(threads, items);
+    const size_t smem = smem_bytes(p, threads, items);
     return p->precision == NOA_DCS_FP64 ? noa_dcs_batched_occupancy64(p->process, threads, smem)
                                         : noa_dcs_batched_occupancy32(p->process, threads, smem);
 }
@@ -80,7 +82,7 @@ int launch(noa_dcs_batch_plan *p, double *out, const double *K, const double *q,
     long long grid = (long long)p->sms * p->ctas_per_sm;
     if (grid > tiles)
         grid = tiles > 0 ? tiles : 1;
-    const size_t smem = smem_bytes(p->threads, p->items);
+    const size_t smem = smem_bytes(p, p->threads, p->items);
     e = p->precision == NOA_DCS_FP64
             ? noa_dcs_batched_launch64(p->process, p->threads, &p->params, (int)grid, smem, s)
             : noa_dcs_batched_launch32(p->process, p->threads, &p->params, (int)grid, smem, s);

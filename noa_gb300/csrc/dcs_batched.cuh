@@ -12,7 +12,9 @@
  *  - Inside a CTA the tile goes through the same compaction as the
  *    single-element kernels: open pairs are appended to a shared-memory work
  *    queue that is popped 256 (THREADS) at a time; for FP32C, pairs whose error
- *    estimate exceeds the tolerance go to a redo queue evaluated in FP64.
+ *    estimate exceeds the tolerance go to a redo queue evaluated in FP64
+ *    (pair production: evaluated again with its screening log in float-float
+ *    arithmetic, and only what that still rejects in FP64).
  *    When the next tile belongs to another segment the queues are drained
  *    first, so every warp evaluates pairs of a single element and the element
  *    constants stay warp-uniform (they are read from the parameter space).
@@ -109,13 +111,61 @@ __device__ __forceinline__ int batch_scan(int v, int *warp_tot, int *total) {
 }
 
 // Shared memory of one CTA: work queue of capacity items*THREADS + THREADS,
-// then the redo queue (2*THREADS), as dynamic shared memory.
+// then the redo queue (2*THREADS), then for FP32C pair production the third
+// queue (2*THREADS) of the pairs its float-float redo step still rejects, as
+// dynamic shared memory.
 template <int THREADS>
 struct BatchSmem {
-    static __host__ __device__ size_t bytes(int items) {
-        return (size_t)(items * THREADS + THREADS) * 24 + (size_t)(2 * THREADS) * 24;
+    static __host__ __device__ size_t bytes(int items, bool third) {
+        return (size_t)(items * THREADS + THREADS) * 24 + (size_t)(2 * THREADS) * 24 +
+               (third ? (size_t)(2 * THREADS) * 24 : 0);
     }
 };
+
+__host__ __device__ constexpr bool batch_third_queue(int proc, int prec) {
+    return proc == NOA_DCS_PROC_PPROD && prec != NOA_DCS_FP64;
+}
+
+// Appends (k, q, i) of the lanes with `push` to a queue (warp-aggregated).
+__device__ __forceinline__ void batch_push(bool push, double k, double q, int64_t i, double *QK, double *QQ,
+                                           int64_t *QI, int *qn) {
+    const unsigned m = __ballot_sync(0xffffffffu, push);
+    if (m) {
+        const int lane = threadIdx.x & 31;
+        int base = 0;
+        if (lane == 0)
+            base = atomicAdd(qn, __popc(m));
+        base = __shfl_sync(0xffffffffu, base, 0);
+        if (push) {
+            const int pos = base + __popc(m & ((1u << lane) - 1u));
+            QK[pos] = k;
+            QQ[pos] = q;
+            QI[pos] = i;
+        }
+    }
+}
+
+// Pair production, FP32C: evaluates redo-queue entry e (if valid) with the
+// float-float screening log; pairs whose estimate still exceeds tol go to the
+// third queue.
+__device__ __forceinline__ void batch_fine_step(double *rK, double *rQ, int64_t *rI, double *xK, double *xQ,
+                                                int64_t *xI, int *xn, int e, bool valid, double *out,
+                                                const noa_dcs_consts &c, float tol) {
+    bool redo = false;
+    double k = 0., q = 0.;
+    int64_t i = 0;
+    if (valid) {
+        k = rK[e];
+        q = rQ[e];
+        i = rI[e];
+        float est;
+        const double v = pprod_fp32c<false, true>(k, q, c, est);
+        redo = !(est <= tol);
+        if (!redo)
+            out[i] = v;
+    }
+    batch_push(redo, k, q, i, xK, xQ, xI, xn);
+}
 
 // One evaluation step over work-queue entry e: FP64 writes directly; FP32C
 // writes or appends to the redo queue.
@@ -141,20 +191,7 @@ __device__ __forceinline__ void batch_step(double *wK, double *wQ, int64_t *wI, 
         if (!redo)
             out[i] = v;
     }
-    const unsigned m = __ballot_sync(0xffffffffu, redo);
-    if (m) {
-        const int lane = threadIdx.x & 31;
-        int base = 0;
-        if (lane == 0)
-            base = atomicAdd(rn, __popc(m));
-        base = __shfl_sync(0xffffffffu, base, 0);
-        if (redo) {
-            const int pos = base + __popc(m & ((1u << lane) - 1u));
-            rK[pos] = k;
-            rQ[pos] = q;
-            rI[pos] = i;
-        }
-    }
+    batch_push(redo, k, q, i, rK, rQ, rI, rn);
 }
 
 template <int PROC, int PREC, int THREADS>
@@ -168,15 +205,21 @@ __global__ void __launch_bounds__(THREADS) dcs_batched_kernel(const __grid_const
     double *rK = reinterpret_cast<double *>(wI + qcap);
     double *rQ = rK + 2 * THREADS;
     int64_t *rI = reinterpret_cast<int64_t *>(rQ + 2 * THREADS);
+    double *xK = reinterpret_cast<double *>(rI + 2 * THREADS);  // third queue (batch_third_queue only)
+    double *xQ = xK + 2 * THREADS;
+    int64_t *xI = reinterpret_cast<int64_t *>(xQ + 2 * THREADS);
+    constexpr bool third = batch_third_queue(PROC, PREC);
     __shared__ int warp_tot[THREADS / 32];
     __shared__ int tile_open;
-    __shared__ int rn;
+    __shared__ int rn, xn;
     __shared__ unsigned long long s_tile;
 
     const int tile_size = items * THREADS;
     const long long total_tiles = p.tile_begin[p.n_seg];
-    if (threadIdx.x == 0)
+    if (threadIdx.x == 0) {
         rn = 0;
+        xn = 0;
+    }
     int qn = 0;
     int cur = -1;
     for (;;) {
@@ -215,13 +258,31 @@ __global__ void __launch_bounds__(THREADS) dcs_batched_kernel(const __grid_const
                     const int r = rn;
                     if (r >= THREADS || (flush && qn == 0 && r > 0)) {
                         const int take = r < THREADS ? r : THREADS;
-                        if ((int)threadIdx.x < take) {
+                        if (third) {
+                            batch_fine_step(rK, rQ, rI, xK, xQ, xI, &xn, r - take + threadIdx.x,
+                                            (int)threadIdx.x < take, p.out, cc, p.tol);
+                        } else if ((int)threadIdx.x < take) {
                             const int e = r - take + threadIdx.x;
                             p.out[rI[e]] = batch_eval64<PROC>(rK[e], rQ[e], cc);
                         }
                         __syncthreads();
                         if (threadIdx.x == 0)
                             rn = r - take;
+                        __syncthreads();
+                        did = true;
+                    }
+                }
+                if (third) {
+                    const int x = xn;
+                    if (x >= THREADS || (flush && qn == 0 && rn == 0 && x > 0)) {
+                        const int take = x < THREADS ? x : THREADS;
+                        if ((int)threadIdx.x < take) {
+                            const int e = x - take + threadIdx.x;
+                            p.out[xI[e]] = batch_eval64<PROC>(xK[e], xQ[e], cc);
+                        }
+                        __syncthreads();
+                        if (threadIdx.x == 0)
+                            xn = x - take;
                         __syncthreads();
                         did = true;
                     }

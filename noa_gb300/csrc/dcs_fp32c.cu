@@ -13,9 +13,13 @@
  *      of its relative error; results within `tol` are written, the others
  *      are appended (warp-aggregated) to a shared-memory redo queue;
  *   3. whenever the redo queue holds 256 pairs, each thread pops one and
- *      evaluates it in FP64 (dcs_fp64.cuh).
+ *      evaluates it in FP64 (dcs_fp64.cuh) -- except for pair production,
+ *      whose redo pairs are evaluated again in FP32 with the screening log in
+ *      float-float arithmetic (pprod_fp32c<false, true>); the ~1% of those
+ *      still above `tol` go to a third queue, evaluated in FP64 in batches of
+ *      256 the same way.
  *
- * FP64 work is thus proportional to the redo fraction (0-4% of open pairs
+ * FP64 work is thus proportional to the redo fraction (0-0.5% of open pairs
  * at tol = 1e-6), and every warp of every phase runs with all lanes busy.
  * No global scratch.
  */
@@ -105,21 +109,49 @@ __device__ __forceinline__ int scan_block(int v, int *warp_tot, int *total) {
     return warp_tot[warp] + x - v;
 }
 
+// The third queue exists for pair production only.
+template <int PROC>
+constexpr int f32_xcap() {
+    return PROC == NOA_DCS_PROC_PPROD ? F_RCAP : 1;
+}
+
+template <int PROC>
 struct Queues {
     double wK[F_QCAP], wQ[F_QCAP];
     int64_t wI[F_QCAP];
     double rK[F_RCAP], rQ[F_RCAP];
     int64_t rI[F_RCAP];
+    double xK[f32_xcap<PROC>()], xQ[f32_xcap<PROC>()];
+    int64_t xI[f32_xcap<PROC>()];
     int warp_tot[F_THREADS / 32];
     int tile_open;
-    int rn;
+    int rn, xn;
 };
+
+// Appends (k, q, i) of the lanes with `push` to a queue (warp-aggregated).
+__device__ __forceinline__ void push_queue(bool push, double k, double q, int64_t i, double *QK, double *QQ,
+                                           int64_t *QI, int *qn) {
+    const unsigned m = __ballot_sync(0xffffffffu, push);
+    if (m) {
+        const int lane = threadIdx.x & 31;
+        int base = 0;
+        if (lane == 0)
+            base = atomicAdd(qn, __popc(m));
+        base = __shfl_sync(0xffffffffu, base, 0);
+        if (push) {
+            const int pos = base + __popc(m & ((1u << lane) - 1u));
+            QK[pos] = k;
+            QQ[pos] = q;
+            QI[pos] = i;
+        }
+    }
+}
 
 // Evaluates work-queue entry e (if valid) in FP32 and appends it to the redo
 // queue when its error estimate exceeds tol.
 template <int PROC>
-__device__ __forceinline__ void fp32_step(Queues &s, int e, bool valid, double *out, const noa_dcs_consts &c,
-                                          float tol) {
+__device__ __forceinline__ void fp32_step(Queues<PROC> &s, int e, bool valid, double *out,
+                                          const noa_dcs_consts &c, float tol) {
     bool redo = false;
     double k = 0., q = 0.;
     int64_t i = 0;
@@ -133,29 +165,40 @@ __device__ __forceinline__ void fp32_step(Queues &s, int e, bool valid, double *
         if (!redo)
             out[i] = v;
     }
-    const unsigned m = __ballot_sync(0xffffffffu, redo);
-    if (m) {
-        const int lane = threadIdx.x & 31;
-        int base = 0;
-        if (lane == 0)
-            base = atomicAdd(&s.rn, __popc(m));
-        base = __shfl_sync(0xffffffffu, base, 0);
-        if (redo) {
-            const int pos = base + __popc(m & ((1u << lane) - 1u));
-            s.rK[pos] = k;
-            s.rQ[pos] = q;
-            s.rI[pos] = i;
-        }
+    push_queue(redo, k, q, i, s.rK, s.rQ, s.rI, &s.rn);
+}
+
+// Pair production: evaluates redo-queue entry e (if valid) with the
+// float-float screening log and appends it to the third queue when its
+// estimate still exceeds tol.
+template <int PROC>
+__device__ __forceinline__ void fine_step(Queues<PROC> &s, int e, bool valid, double *out,
+                                          const noa_dcs_consts &c, float tol) {
+    bool redo = false;
+    double k = 0., q = 0.;
+    int64_t i = 0;
+    if (valid) {
+        k = s.rK[e];
+        q = s.rQ[e];
+        i = s.rI[e];
+        float est;
+        const double v = pprod_fp32c<false, true>(k, q, c, est);
+        redo = !(est <= tol);
+        if (!redo)
+            out[i] = v;
     }
+    push_queue(redo, k, q, i, s.xK, s.xQ, s.xI, &s.xn);
 }
 
 template <int PROC>
 __global__ void __launch_bounds__(F_THREADS, f32_min_ctas<PROC>()) dcs_fp32c_kernel(const double *__restrict__ K,
                                                               const double *__restrict__ q, double *out, int64_t n,
                                                               const noa_dcs_consts c, float tol) {
-    __shared__ Queues s;
-    if (threadIdx.x == 0)
+    __shared__ Queues<PROC> s;
+    if (threadIdx.x == 0) {
         s.rn = 0;
+        s.xn = 0;
+    }
     int qn = 0;
     int64_t base = (int64_t)blockIdx.x * F_TILE;
     for (;;) {
@@ -189,8 +232,9 @@ __global__ void __launch_bounds__(F_THREADS, f32_min_ctas<PROC>()) dcs_fp32c_ker
             qn += s.tile_open;
             base += (int64_t)gridDim.x * F_TILE;
         }
-        // One call site each for the FP32 step and the FP64 redo (see the
-        // FP64 kernels): full batches while tiles remain, everything at the end.
+        // One call site each for the FP32 step, the redo step and the FP64
+        // evaluation (see the FP64 kernels): full batches while tiles remain,
+        // everything at the end.
         for (;;) {
             bool did = false;
             if (qn >= F_THREADS || (!more && qn > 0)) {
@@ -203,7 +247,9 @@ __global__ void __launch_bounds__(F_THREADS, f32_min_ctas<PROC>()) dcs_fp32c_ker
             const int rn = s.rn;
             if (rn >= F_THREADS || (!more && qn == 0 && rn > 0)) {
                 const int take = rn < F_THREADS ? rn : F_THREADS;
-                if ((int)threadIdx.x < take) {
+                if (PROC == NOA_DCS_PROC_PPROD) {
+                    fine_step<PROC>(s, rn - take + threadIdx.x, (int)threadIdx.x < take, out, c, tol);
+                } else if ((int)threadIdx.x < take) {
                     const int e = rn - take + threadIdx.x;
                     out[s.rI[e]] = eval64<PROC>(s.rK[e], s.rQ[e], c);
                 }
@@ -212,6 +258,21 @@ __global__ void __launch_bounds__(F_THREADS, f32_min_ctas<PROC>()) dcs_fp32c_ker
                     s.rn = rn - take;
                 __syncthreads();
                 did = true;
+            }
+            if (PROC == NOA_DCS_PROC_PPROD) {
+                const int xn = s.xn;
+                if (xn >= F_THREADS || (!more && qn == 0 && s.rn == 0 && xn > 0)) {
+                    const int take = xn < F_THREADS ? xn : F_THREADS;
+                    if ((int)threadIdx.x < take) {
+                        const int e = xn - take + threadIdx.x;
+                        out[s.xI[e]] = eval64<PROC>(s.xK[e], s.xQ[e], c);
+                    }
+                    __syncthreads();
+                    if (threadIdx.x == 0)
+                        s.xn = xn - take;
+                    __syncthreads();
+                    did = true;
+                }
             }
             if (!did)
                 break;

@@ -149,6 +149,74 @@ NOA_HD void f_exp_split_aff(float ch, float cl, float hh, float hl, float xh, fl
     em1 = fmaf(eh, ul, expm1f(uh));
 }
 
+// ---------------------------------------------------------------- float-float exp / log
+// 2^(j/64), j = 0..63, as float pairs hi + lo (to ~2^-48), for ff_exp.
+NOA_F32_TABLE float kExp64H[64] = {
+    1.000000000e+00f, 1.010889292e+00f, 1.021897197e+00f, 1.033024907e+00f, 1.044273734e+00f, 1.055645227e+00f,
+    1.067140460e+00f, 1.078760743e+00f, 1.090507746e+00f, 1.102382541e+00f, 1.114386797e+00f, 1.126521587e+00f,
+    1.138788581e+00f, 1.151189208e+00f, 1.163724899e+00f, 1.176396966e+00f, 1.189207077e+00f, 1.202156782e+00f,
+    1.215247393e+00f, 1.228480577e+00f, 1.241857767e+00f, 1.255380750e+00f, 1.269050956e+00f, 1.282870054e+00f,
+    1.296839595e+00f, 1.310961246e+00f, 1.325236678e+00f, 1.339667559e+00f, 1.354255557e+00f, 1.369002461e+00f,
+    1.383909941e+00f, 1.398979664e+00f, 1.414213538e+00f, 1.429613352e+00f, 1.445180774e+00f, 1.460917830e+00f,
+    1.476826191e+00f, 1.492907763e+00f, 1.509164453e+00f, 1.525598168e+00f, 1.542210817e+00f, 1.559004426e+00f,
+    1.575980902e+00f, 1.593142152e+00f, 1.610490322e+00f, 1.628027439e+00f, 1.645755529e+00f, 1.663676620e+00f,
+    1.681792855e+00f, 1.700106382e+00f, 1.718619347e+00f, 1.737333894e+00f, 1.756252170e+00f, 1.775376439e+00f,
+    1.794709086e+00f, 1.814252138e+00f, 1.834008098e+00f, 1.853979111e+00f, 1.874167681e+00f, 1.894575953e+00f,
+    1.915206552e+00f, 1.936061740e+00f, 1.957144141e+00f, 1.978456020e+00f};
+NOA_F32_TABLE float kExp64L[64] = {
+    0.000000000e+00f, -5.711605411e-09f, -4.811559862e-08f, -2.809089317e-08f, 4.833470157e-08f,
+    -4.907169426e-08f, -5.933751979e-08f, 5.461594554e-08f, -1.307753994e-08f, 4.260501996e-08f,
+    -5.435540018e-08f, 3.123641434e-08f, 5.386222313e-08f, 2.192228266e-08f, -4.051441493e-08f,
+    2.566975077e-08f, 3.797635273e-08f, -5.069756526e-08f, -3.267394888e-08f, -4.136200360e-08f,
+    4.496838102e-08f, 7.322237483e-09f, 1.419333318e-09f, -3.816621685e-08f, -4.018999533e-08f,
+    -3.496571566e-08f, -3.496373324e-08f, -3.461673970e-08f, -1.012334927e-08f, -3.845881835e-08f,
+    -5.875577358e-08f, 8.689434061e-09f, 2.420323497e-08f, -1.342992917e-08f, 3.324199938e-08f,
+    -3.628657552e-08f, -4.500898854e-08f, -3.423620143e-08f, -2.495937323e-08f, -1.762856883e-08f,
+    8.070904833e-09f, -2.576466507e-08f, -5.661025426e-08f, -4.903136785e-10f, 9.836217174e-09f,
+    -1.726008314e-08f, -5.124972091e-08f, -3.920298752e-08f, -2.475532668e-08f, -2.865147231e-08f,
+    -4.849617596e-08f, -5.850223417e-08f, -9.235770371e-09f, 5.343197884e-08f, -1.141504491e-08f,
+    3.736258236e-08f, -1.123927795e-08f, 1.436561181e-08f, -4.663005626e-08f, 2.810338451e-08f,
+    9.845328108e-09f, 5.357072297e-08f, -1.702180441e-08f, 6.032726318e-09f};
+
+// 2^n as a float, -126 <= n <= 127.
+NOA_HD float f_pow2i(int n) {
+#if defined(__CUDA_ARCH__)
+    return __int_as_float((n + 127) << 23);
+#else
+    return ldexpf(1.f, n);
+#endif
+}
+
+// exp(a) of a float-float a, -87 < a < 88, to ~2^-44 relative on the FP32
+// pipe (Tang's table method): a = k ln2/64 + r with ln2/64 in three parts
+// (Cody-Waite; k L1 is exact for |k| < 2^13), exp(r) - 1 = r + r^2/2 + r^3/6
+// + r^4/24 + r^5/120 (|r| <= 0.0055, r^2 in float-float, the cubic tail in
+// float), times 2^(j/64) from the table (j = k mod 64) and 2^(k div 64).
+NOA_HD FF ff_exp(FF a) {
+    const float kf = rintf(a.h * 92.33248262f);  // 64 / ln 2
+    const int k = (int)kf;
+    const float r1 = fmaf(-kf, 0.010833740234375f, a.h);  // exact
+    const float ph = kf * -3.315538152e-06f;
+    const float pl = fmaf(kf, -3.315538152e-06f, -ph);
+    const FF r = ff_add(FF{r1, fmaf(-kf, 2.572804640e-14f, a.l)}, FF{-ph, -pl});
+    const float rh = r.h;
+    const float tail = rh * rh * rh * fmaf(rh, fmaf(rh, 1.f / 120.f, 1.f / 24.f), 1.f / 6.f);
+    const FF r2 = ff_mul(r, r);
+    const FF em1 = ff_add(r, ff_add(FF{0.5f * r2.h, 0.5f * r2.l}, FF{tail, 0.f}));
+    const FF T{kExp64H[k & 63], kExp64L[k & 63]};
+    const FF e = ff_add(T, ff_mul(T, em1));
+    const float sc = f_pow2i(k >> 6);
+    return FF{e.h * sc, e.l * sc};
+}
+
+// log(x) of a positive normal float-float x to ~2^-44 relative: the float
+// log, corrected by t = x exp(-y0) - 1 (log(1 + t) = t - t^2/2, |t| ~ 1e-7).
+NOA_HD FF ff_log(FF x) {
+    const float y0 = logf(x.h);
+    const FF t = ff_add(ff_mul(x, ff_exp(FF{-y0, 0.f})), FF{-1.f, 0.f});
+    return ff_add(FF{y0, 0.f}, ff_add(t, FF{-0.5f * t.h * t.h, 0.f}));
+}
+
 // ---------------------------------------------------------------- bremsstrahlung
 NOA_HD double brems_fp32c(double K, double q, const noa_dcs_consts &c, float &est) {
     est = 0.f;
@@ -187,7 +255,15 @@ NOA_HD double brems_fp32c(double K, double q, const noa_dcs_consts &c, float &es
 // CHECKED = false: the caller has already established with the exact bounds
 // that the pair is open, and argmin is then formed in lean arithmetic (its
 // relative error only matters for |tmin| < 1e-6, which is sent to FP64).
-template <bool CHECKED = true>
+//
+// FINE = true: the screening log Le and what it is built from (eps, xi, Ye,
+// xe, the log arguments) in float-float arithmetic, the rest as in the float
+// form.  Le is small (0.05-0.5) where Be Le carries the node, and its float
+// absolute error of a few 2^-24 (from Ye's log and the chain before it) is
+// what sends ~4% of the open pairs past a 1e-6 estimate; with Le to ~1e-13
+// relative about one in a hundred of those stays above it.  About twice the
+// FP32 work of the float form, for the pairs the float form rejects.
+template <bool CHECKED = true, bool FINE = false>
 NOA_HD double pprod_fp32c(double K, double q, const noa_dcs_consts &c, float &est) {
     est = 0.f;
     double argmin;
@@ -216,6 +292,18 @@ NOA_HD double pprod_fp32c(double K, double q, const noa_dcs_consts &c, float &es
     const float AZ13 = fpconv::f32(c.pp_AZ13), cL = fpconv::f32(c.pp_cL), cLe = fpconv::f32(c.pp_cLe);
     const float rAZ13 = fpconv::f32(c.pp_r_AZ13), Z13_15 = fpconv::f32(c.pp_15_Z13), inv_r2 = fpconv::f32(c.pp_inv_r2);
     const float b2 = 2.f * beta, b15 = 1.5f * beta, b3 = 3.f * beta, b4 = 4.f * beta;
+
+    // float-float inputs of the screening log (FINE only)
+    FF tminF{}, betaF{}, xfF{}, qF{}, cLF{}, cLeF{}, aq2F{};
+    if (FINE) {
+        tminF = FF{tmin, tmin_lo};
+        betaF = ff_from(beta_d);
+        xfF = ff_from(c.pp_half_r2 * beta_d);
+        qF = ff_from(q);
+        cLF = ff_from(c.pp_cL);
+        cLeF = ff_from(c.pp_cLe);
+        aq2F = ff_mul(ff_from(c.pp_AZ13 * c.pp_AZ13), ff_mul(qF, qF));
+    }
 
     KSum I;
     float err = 0.f;
@@ -256,9 +344,28 @@ NOA_HD double pprod_fp32c(double K, double q, const noa_dcs_consts &c, float &es
                                                                   b2 * (2.f - rho2));
         const float xe = opxi * (1.f + Ye);
         const float cLi = cL * f_rcp(rho21);
-        const float r1 = AZ13 * qf * f_rcp(qf + cLi * xe);
-        const float r2 = xe * f_rcp(1.f + cLe * xe);
-        const float Le = 0.5f * logf(r1 * r1 * r2);
+        float Le;
+        if (FINE) {
+            // Le = log(AZ13 q sqrt(xe) / D1) - log(D2) / 2 (dcs.hh:199-202) as one
+            // float-float log of AZ13^2 q^2 xe / (D1^2 D2)
+            const FF epsF = ff_exp(ff_mul(FF{kF8XH[j], kF8XL[j]}, tminF));
+            const FF rhoF = ff_add(1.f, ff_neg(epsF));
+            const FF rho2F = ff_mul(rhoF, rhoF);
+            const FF r21F = ff_mul(epsF, ff_add(2.f, ff_neg(epsF)));
+            const FF xiF = ff_mul(xfF, r21F);
+            const FF L3 = ff_log(ff_add(3.f, ff_div(FF{1.f, 0.f}, xiF)));
+            const FF num = ff_add(ff_add(5.f, ff_neg(rho2F)), ff_mul(ff_mul(4.f, betaF), ff_add(1.f, rho2F)));
+            const FF den = ff_add(ff_add(ff_mul(ff_mul(2.f, ff_add(1.f, ff_mul(3.f, betaF))), L3), ff_neg(rho2F)),
+                                  ff_neg(ff_mul(ff_mul(2.f, betaF), ff_add(2.f, ff_neg(rho2F)))));
+            const FF xeF = ff_mul(ff_add(1.f, xiF), ff_add(1.f, ff_div(num, den)));
+            const FF d1 = ff_add(qF, ff_mul(ff_div(cLF, r21F), xeF));
+            const FF lg = ff_log(ff_div(ff_mul(aq2F, xeF), ff_mul(ff_mul(d1, d1), ff_add(1.f, ff_mul(cLeF, xeF)))));
+            Le = 0.5f * (lg.h + lg.l);
+        } else {
+            const float r1 = AZ13 * qf * f_rcp(qf + cLi * xe);
+            const float r2 = xe * f_rcp(1.f + cLe * xe);
+            Le = 0.5f * logf(r1 * r1 * r2);
+        }
         const float Phi_e = f_clamp0(Be * Le);
 
         float Bmu, eBmu;
@@ -286,9 +393,10 @@ NOA_HD double pprod_fp32c(double K, double q, const noa_dcs_consts &c, float &es
         const float Phi_mu = f_clamp0(Bmu * Lmu);
         const float g = -(Phi_e + Phi_mu * inv_r2) * eps * tmin;
         I.add(g * kF8W[j]);
-        // error of this node: the logs (Le, Lmu) to ~2 u absolute, the B terms as tracked, the rest ~3 u relative
+        // error of this node: the logs (Le, Lmu) to ~2 u absolute (Le to 0.5 u
+        // relative when FINE), the B terms as tracked, the rest ~3 u relative
         const float eg = fabsf(eps * tmin) *
-                         ((Phi_e > 0.f ? fabsf(Be) * 2.f * U32 + fabsf(Le) * eBe : 0.f) +
+                         ((Phi_e > 0.f ? fabsf(Be) * (FINE ? fabsf(Le) : 2.f) * U32 + fabsf(Le) * eBe : 0.f) +
                           (Phi_mu > 0.f ? (fabsf(Bmu) * 2.f * U32 + fabsf(Lmu) * eBmu) * inv_r2 : 0.f)) +
                          fabsf(g) * 3.f * U32;
         err += eg * kF8W[j];

@@ -27,7 +27,9 @@
  *     A lo 64 (512 for the two).
  *     DCS = exp(baseline + residual), in float (1e-6 relative).
  *  3. fallback: the FP32C evaluation (dcs_fp32c.cuh) of the fallback list,
- *     with FP64 (dcs_fp64.cuh) for pairs above its tolerance.
+ *     with FP64 (dcs_fp64.cuh) for pairs above its tolerance (pair
+ *     production: after a second FP32 pass with the float-float screening
+ *     log).
  *
  * Every mbarrier wait is bounded; on expiry the kernel records
  * NOA_DCS_ERROR_TIMEOUT in the model's status word, gives the MMAs still in
@@ -224,16 +226,39 @@ __global__ void __launch_bounds__(256) netprep_kernel(const __grid_constant__ In
     }
 }
 
+// Appends (index, segment) of the lanes with `push` to a shared-memory queue
+// (warp-aggregated).
+__device__ __forceinline__ void push_index(bool push, int32_t i, uint8_t sg, int32_t *q, uint8_t *qs, int *qn) {
+    const unsigned m = __ballot_sync(0xffffffffu, push);
+    if (m) {
+        const int lane = threadIdx.x & 31;
+        int at = 0;
+        if (lane == 0)
+            at = atomicAdd(qn, __popc(m));
+        at = __shfl_sync(0xffffffffu, at, 0);
+        if (push) {
+            const int pos = at + __popc(m & ((1u << lane) - 1u));
+            q[pos] = i;
+            qs[pos] = sg;
+        }
+    }
+}
+
 // FP32C evaluation of the fallback list; pairs above the tolerance go to a
 // shared-memory redo queue that full warps drain in FP64, so the FP64 work is
 // proportional to the redo fraction (as in dcs_fp32c.cu).
 template <int PROC>
 __global__ void __launch_bounds__(256) fallback_kernel(const __grid_constant__ InferParams p) {
-    __shared__ int32_t rq[512];
-    __shared__ uint8_t rs[512];
-    __shared__ int rn;
-    if (threadIdx.x == 0)
+    // pair production: redo pairs are evaluated again with the float-float
+    // screening log, and the few it still rejects go to a third queue (FP64)
+    constexpr bool fine = PROC == NOA_DCS_PAIR_PRODUCTION;
+    __shared__ int32_t rq[512], xq[fine ? 512 : 1];
+    __shared__ uint8_t rs[512], xs[fine ? 512 : 1];
+    __shared__ int rn, xn;
+    if (threadIdx.x == 0) {
         rn = 0;
+        xn = 0;
+    }
     __syncthreads();
     const unsigned long long cnt = p.counters[1];
     for (unsigned long long base = (unsigned long long)blockIdx.x * blockDim.x; base < cnt;
@@ -254,34 +279,59 @@ __global__ void __launch_bounds__(256) fallback_kernel(const __grid_constant__ I
             if (!redo)
                 p.out[i] = v;
         }
-        const unsigned m = __ballot_sync(0xffffffffu, redo);
-        if (m) {
-            const int lane = threadIdx.x & 31;
-            int at = 0;
-            if (lane == 0)
-                at = atomicAdd(&rn, __popc(m));
-            at = __shfl_sync(0xffffffffu, at, 0);
-            if (redo) {
-                const int pos = at + __popc(m & ((1u << lane) - 1u));
-                rq[pos] = i;
-                rs[pos] = sg;
-            }
-        }
+        push_index(redo, i, sg, rq, rs, &rn);
         __syncthreads();
         const bool last = base + (unsigned long long)gridDim.x * blockDim.x >= cnt;
-        while (rn >= (last ? 1 : 256)) {
-            const int n = rn, take = n < 256 ? n : 256;
-            if ((int)threadIdx.x < take) {
-                const int k = n - take + threadIdx.x;
-                const int32_t j = rq[k];
-                const noa_dcs_consts &c = p.consts[rs[k]];
-                p.out[j] = PROC == NOA_DCS_PAIR_PRODUCTION ? noa_dcs::pprod_fp64(p.K[j], p.q[j], c)
-                                                           : noa_dcs::photo_fp64(p.K[j], p.q[j], c);
+        // one call site each for the redo evaluation and the FP64 one
+        for (;;) {
+            bool did = false;
+            const int n = rn;
+            if (n >= (last ? 1 : 256)) {
+                const int take = n < 256 ? n : 256;
+                bool again = false;
+                int32_t j = 0;
+                uint8_t sj = 0;
+                if ((int)threadIdx.x < take) {
+                    const int k = n - take + threadIdx.x;
+                    j = rq[k];
+                    sj = rs[k];
+                    const noa_dcs_consts &c = p.consts[sj];
+                    if (fine) {
+                        float est;
+                        const double v = noa_dcs::pprod_fp32c<false, true>(p.K[j], p.q[j], c, est);
+                        again = !(est <= p.tol);
+                        if (!again)
+                            p.out[j] = v;
+                    } else {
+                        p.out[j] = noa_dcs::photo_fp64(p.K[j], p.q[j], c);
+                    }
+                }
+                if (fine)
+                    push_index(again, j, sj, xq, xs, &xn);
+                __syncthreads();
+                if (threadIdx.x == 0)
+                    rn = n - take;
+                __syncthreads();
+                did = true;
             }
-            __syncthreads();
-            if (threadIdx.x == 0)
-                rn = n - take;
-            __syncthreads();
+            if (fine) {
+                const int nx = xn;
+                if (nx >= 256 || (last && rn == 0 && nx > 0)) {
+                    const int take = nx < 256 ? nx : 256;
+                    if ((int)threadIdx.x < take) {
+                        const int k = nx - take + threadIdx.x;
+                        const int32_t j = xq[k];
+                        p.out[j] = noa_dcs::pprod_fp64(p.K[j], p.q[j], p.consts[xs[k]]);
+                    }
+                    __syncthreads();
+                    if (threadIdx.x == 0)
+                        xn = nx - take;
+                    __syncthreads();
+                    did = true;
+                }
+            }
+            if (!did)
+                break;
         }
     }
 }
