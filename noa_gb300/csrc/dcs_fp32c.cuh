@@ -266,26 +266,27 @@ NOA_HD double brems_fp32c(double K, double q, const noa_dcs_consts &c, float &es
 template <bool CHECKED = true, bool FINE = false>
 NOA_HD double pprod_fp32c(double K, double q, const noa_dcs_consts &c, float &est) {
     est = 0.f;
-    double argmin;
+    FF argmin;
     if (CHECKED) {
         if (q <= 4. * ME)
             return 0.;
         if (q >= K + c.pp_kmax_shift)
             return 0.;
-        argmin = pprod_argmin_exact(K, q, c);
-        if ((argmin >= 1.) || (argmin <= 0.))
+        const double a = pprod_argmin_exact(K, q, c);
+        if ((a >= 1.) || (a <= 0.))
             return 0.;
+        argmin = ff_from(a);
     } else {
-        argmin = ff_to_double(pprod_argmin_ff(K, q, c));
+        argmin = pprod_argmin_ff(K, q, c);
     }
     const double mass = c.mass;
     const double E = K + mass;
     const double Emq = E - q;
     // beta = 0.5 nu^2 / (1 - nu) = 0.5 q^2 / (E (E - q))
     const double beta_d = 0.5 * q * q * d_rcp(E * Emq);
-    const double tmin_d = d_log(argmin);
-    const float tmin = fpconv::f32(tmin_d);
-    const float tmin_lo = fpconv::f32(tmin_d - fpconv::f64(tmin));  // tmin = tmin + tmin_lo to ~2^-48
+    // tmin = log(argmin) = tmin + tmin_lo, float-float log (~2^-44, no FP64)
+    const FF tminF0 = ff_log(argmin);
+    const float tmin = tminF0.h, tmin_lo = tminF0.l;
     const float beta = fpconv::f32(beta_d);
     const float xi_factor = fpconv::f32(c.pp_half_r2 * beta_d);
     const float qf = fpconv::f32(q);
@@ -296,7 +297,7 @@ NOA_HD double pprod_fp32c(double K, double q, const noa_dcs_consts &c, float &es
     // float-float inputs of the screening log (FINE only)
     FF tminF{}, betaF{}, xfF{}, qF{}, cLF{}, cLeF{}, aq2F{};
     if (FINE) {
-        tminF = FF{tmin, tmin_lo};
+        tminF = tminF0;
         betaF = ff_from(beta_d);
         xfF = ff_from(c.pp_half_r2 * beta_d);
         qF = ff_from(q);

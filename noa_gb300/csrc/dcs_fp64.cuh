@@ -113,16 +113,36 @@ static __device__ __noinline__ bool pprod_live_tail(double K, double q, double m
 }
 
 __device__ __forceinline__ bool pprod_live(double K, double q, const noa_dcs_consts &c) {
-    if (q <= 4. * ME)
+    const float Kf = fpconv::f32(K), qf = fpconv::f32(q);
+    if (!(Kf > 1e-20f && Kf < 1e30f && qf > 1e-20f && qf < 1e30f)) {
+        // outside the float-safe range (and NaN): the reference's IEEE checks
+        if (q <= 4. * ME)
+            return false;
+        if (q >= K + c.pp_kmax_shift)
+            return false;
+        return pprod_live_tail(K, q, c.mass, c.inv_mass_h, c.inv_mass_l, 1.f);
+    }
+    // q <= 4 me and q >= K + m (1 - 0.75 sqrt(e) Z^1/3) (dcs.hh:151-156) in
+    // float, with the IEEE comparison within a relative margin of 1e-5
+    constexpr float four_me = (float)(4. * ME);
+    if (qf < four_me * 0.99999f)
         return false;
-    if (q >= K + c.pp_kmax_shift)
+    if (!(qf > four_me * 1.00001f) && q <= 4. * ME)
         return false;
-    // argmin in float (K - q formed in double: gamma - q/m = 1 + (K - q)/m);
-    // the reference's IEEE value decides only within 1e-5 of a bound
+    const float shift = fpconv::f32(c.pp_kmax_shift);
+    const float ub = Kf + shift, margin = 1e-5f * (Kf + fabsf(shift));
+    if (qf >= ub + margin)
+        return false;
+    if (!(qf <= ub - margin) && q >= K + c.pp_kmax_shift)
+        return false;
+    // argmin in float, with K - q (gamma - q/m = 1 + (K - q)/m) as a
+    // float-float difference; the reference's IEEE value decides only within
+    // 1e-5 of a bound
+    const FF kmq = ff_add(ff_split(K), ff_neg(ff_split(q)));
     const float im = fpconv::f32(c.inv_mass);
-    const float x0 = (float)(4. * ME) * lean64::rcp_approx(fpconv::f32(q));
-    const float gamma = 1.f + fpconv::f32(K) * im;
-    const float x1 = 6.f * lean64::rcp_approx(gamma * (1.f + fpconv::f32(K - q) * im));
+    const float x0 = four_me * lean64::rcp_approx(qf);
+    const float gamma = 1.f + Kf * im;
+    const float x1 = 6.f * lean64::rcp_approx(gamma * (1.f + (kmq.h + kmq.l) * im));
     const float a = (x0 + 2.f * (1.f - x0) * x1) * lean64::rcp_approx(1.f + (1.f - x1) * sqrtf(fmaxf(1.f - x0, 0.f)));
     if (fabsf(a - 1.f) > 1e-5f && a > 1e-30f && a < 1e30f && x0 < 0.9f)
         return a < 1.f;

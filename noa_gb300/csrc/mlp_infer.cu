@@ -120,25 +120,23 @@ __global__ void __launch_bounds__(CL_THREADS) classify_kernel(const __grid_const
                     seg++;
                 const noa_dcs_consts &c = p.consts[seg];
                 const double K = p.K[i], q = p.q[i];
-                if (!open_fast<PROC>(K, q, c)) {
+                const bool open = open_fast<PROC>(K, q, c);
+                // the cell and the features for every pair (few instructions,
+                // no divergence); only the trust lookup and the stores branch
+                const float Kf = fpconv::f32(K);
+                const float lk = logf(Kf), ln = logf(fpconv::f32(q) / (Kf + c.mass_h));
+                const float fk = floorf((lk - p.logk_lo) / p.logk_span * 64.f);
+                const float fn = floorf((ln - p.lognu_lo) / p.lognu_span * 64.f);
+                const bool in_grid = fk >= 0.f && fk < 64.f && fn >= 0.f && fn < 64.f;
+                const bool trusted = open && in_grid && p.trust[(seg * 64 + (int)fk) * 64 + (int)fn] != 0;
+                f.x = (lk - p.norm.in_shift[0]) * p.norm.in_scale[0];
+                f.y = (ln - p.norm.in_shift[1]) * p.norm.in_scale[1];
+                f.z = (p.Zf[seg] * 0.01f - p.norm.in_shift[2]) * p.norm.in_scale[2];
+                f.w = (p.logA[seg] - p.norm.in_shift[3]) * p.norm.in_scale[3];
+                if (!open)
                     p.out[i] = 0.;
-                } else {
-                    const float lk = logf(fpconv::f32(K)), ln = logf(fpconv::f32(q) / fpconv::f32(K + c.mass));
-                    const float fk = floorf((lk - p.logk_lo) / p.logk_span * 64.f);
-                    const float fn = floorf((ln - p.lognu_lo) / p.lognu_span * 64.f);
-                    bool trusted = false;
-                    if (fk >= 0.f && fk < 64.f && fn >= 0.f && fn < 64.f)
-                        trusted = p.trust[(seg * 64 + (int)fk) * 64 + (int)fn] != 0;
-                    if (trusted) {
-                        net_mask |= 1u << j;
-                        f.x = (lk - p.norm.in_shift[0]) * p.norm.in_scale[0];
-                        f.y = (ln - p.norm.in_shift[1]) * p.norm.in_scale[1];
-                        f.z = (p.Zf[seg] * 0.01f - p.norm.in_shift[2]) * p.norm.in_scale[2];
-                        f.w = (p.logA[seg] - p.norm.in_shift[3]) * p.norm.in_scale[3];
-                    } else {
-                        fb_mask |= 1u << j;
-                    }
-                }
+                net_mask |= (unsigned)trusted << j;
+                fb_mask |= (unsigned)(open && !trusted) << j;
             }
             s_feat[j][threadIdx.x] = f;
             s_seg[j][threadIdx.x] = (uint8_t)seg;
