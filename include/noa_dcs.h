@@ -135,7 +135,9 @@ int noa_dcs_cuda_hard_scattering(double *mu0, double *lb_h, const double *G, con
 
 /* FP32-compensated form with an explicit tolerance: every pair whose
  * estimated relative error exceeds `tolerance` (0 < tolerance < 1) is
- * recomputed in FP64.  noa_dcs_cuda_vmap with NOA_DCS_FP32C uses 1e-6.
+ * recomputed in FP64 (pair production: first in FP32 with its screening log
+ * in float-float arithmetic, and in FP64 if that estimate still exceeds
+ * `tolerance`).  noa_dcs_cuda_vmap with NOA_DCS_FP32C uses 1e-6.
  * No counterpart in the reference (which has only FP64). */
 int noa_dcs_cuda_vmap_fp32c(int process, double *result, const double *K, const double *q, int64_t n,
                             const noa_dcs_element *element, double mass, float tolerance, void *stream);
