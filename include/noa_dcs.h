@@ -283,10 +283,12 @@ int noa_dcs_probe_fma(int fp64, void *out, int blocks, int iters, double *flops,
 
 /* Diagnostics (no counterpart in the reference): out[i] = f(x[i]) (or
  * f(x[i], y[i])) for one of the library's FP64 elementary functions --
- * fn 0 log, 1 exp, 2 reciprocal, 3 division x/y, 4 sqrt -- or of its
+ * fn 0 log, 1 exp, 2 reciprocal, 3 division x/y, 4 sqrt -- of its
  * integer-pipe conversions -- fn 5 (double)(float)x, 6 (double)(int)x for x
- * in int range -- on device buffers, so that their error can be measured
- * against a reference libm and the conversions checked against the casts. */
+ * in int range -- or of its float-float functions on x split into a float
+ * pair -- fn 7 exp (-87 < x < 88), 8 log (x > 0, normal float range) -- on
+ * device buffers, so that their error can be measured against a reference
+ * libm and the conversions checked against the casts. */
 int noa_dcs_lean64_eval(int fn, const double *x, const double *y, double *out, int64_t n, void *stream);
 
 #ifdef __cplusplus

@@ -1,9 +1,11 @@
 /*
- * Diagnostics entry point: evaluates one lean64 function (lean64.cuh) or one
- * integer-pipe conversion (fpconv.cuh) element-wise so that tests can bound
- * its error against a host libm, or check it bit for bit against the cast it
- * replaces.  No counterpart in the reference.
+ * Diagnostics entry point: evaluates one lean64 function (lean64.cuh), one
+ * integer-pipe conversion (fpconv.cuh) or one float-float function
+ * (dcs_fp32c.cuh) element-wise so that tests can bound its error against a
+ * host libm, or check it bit for bit against the cast it replaces.  No
+ * counterpart in the reference.
  */
+#include "dcs_fp32c.cuh"
 #include "dcs_launch.h"
 #include "lean64.cuh"
 
@@ -23,7 +25,9 @@ __global__ void lean64_eval_kernel(int fn, const double *__restrict__ x, const d
         case 3: r = lean64::lean_div(a, y[i]); break;
         case 4: r = lean64::lean_sqrt(a); break;
         case 5: r = fpconv::f64(fpconv::f32(a)); break;      // (double)(float)a
-        default: r = fpconv::f64i(__double2int_rz(a)); break;  // (double)(int)a
+        case 6: r = fpconv::f64i(__double2int_rz(a)); break;  // (double)(int)a
+        case 7: r = noa_dcs::ff_to_double(noa_dcs::ff_exp(noa_dcs::ff_from(a))); break;
+        default: r = noa_dcs::ff_to_double(noa_dcs::ff_log(noa_dcs::ff_from(a))); break;
         }
         out[i] = r;
     }
@@ -32,7 +36,7 @@ __global__ void lean64_eval_kernel(int fn, const double *__restrict__ x, const d
 } // namespace
 
 extern "C" int noa_dcs_lean64_eval(int fn, const double *x, const double *y, double *out, int64_t n, void *stream) {
-    if (fn < 0 || fn > 6 || n < 0 || (n > 0 && (!x || !out || (fn == 3 && !y))))
+    if (fn < 0 || fn > 8 || n < 0 || (n > 0 && (!x || !out || (fn == 3 && !y))))
         return NOA_DCS_ERROR_INVALID_VALUE;
     if (n == 0)
         return NOA_DCS_SUCCESS;

@@ -106,3 +106,37 @@ def test_integer_pipe_int_conversion_is_the_cast(cuda_device):
     i = np.concatenate([rng.integers(-(1 << 31), 1 << 31, 200_000), [0, 1, -1, 2**31 - 1, -2**31, 1023, -1074]])
     x = i.astype(np.float64)
     assert np.array_equal(_bits(run(6, x)), _bits(x))
+
+
+def float_pair(x):
+    """x as the float pair h + l of the float-float split, in extended
+    precision (numpy longdouble)."""
+    h = x.astype(np.float32)
+    l_ = (x - h.astype(np.float64)).astype(np.float32)
+    return h.astype(np.longdouble) + l_.astype(np.longdouble)
+
+
+def test_float_float_exp(cuda_device):
+    """ff_exp (Tang's table method on float pairs) to a few 2^-44 of exp of
+    its float-pair input, against numpy's extended-precision exp."""
+    rng = np.random.default_rng(7)
+    x = np.concatenate([rng.uniform(-70, 80, 200000), rng.uniform(-1e-3, 1e-3, 50000), rng.uniform(-25, 0, 200000),
+                        [0.0, 1.0, -1.0, np.log(2.0)]])
+    got = run(7, x).astype(np.longdouble)
+    ref = np.exp(float_pair(x))
+    rel = np.abs((got - ref) / ref).astype(np.float64)
+    assert rel.max() <= 5e-13, rel.max()
+
+
+def test_float_float_log(cuda_device):
+    """ff_log (float log plus one correction through ff_exp): a few 2^-44
+    relative away from 1, ~2^-47 absolute near 1."""
+    rng = np.random.default_rng(8)
+    x = np.concatenate([sample(rng, 200000, 1e-30, 1e30), 3 + sample(rng, 100000, 1e-6, 1e8),
+                        1 + rng.uniform(-1e-3, 1e-3, 100000), [1.0, 2.0, 3.0, 0.5]])
+    got = run(8, x).astype(np.longdouble)
+    ref = np.log(float_pair(x))
+    err = np.abs(got - ref).astype(np.float64)
+    big = np.abs(ref) > 0.1
+    assert (err[big] / np.abs(ref[big]).astype(np.float64)).max() <= 5e-13
+    assert err[~big].max() <= 3e-14
