@@ -72,6 +72,7 @@ typedef struct noa_dcs_consts {
     double ph_q_min;        /* mpi (1 + 0.5 mpi / M) */
     double ph_log_q02;      /* log(Q02 / Lambda2), ALLM */
     double ph_inv_log_q02;  /* 1 / log(Q02 / Lambda2) */
+    double ph_scale;        /* 0.5 cf 1e3 N_A / A, cf = 2.603096e-35 (FP32C final scaling) */
 
     /* ionisation, dcs.hh:408-443 */
     double io_Wmin;         /* 0.62 I */
@@ -147,6 +148,7 @@ static inline void noa_dcs_fill_consts(noa_dcs_consts *c, double A, double I, in
         c->ph_q_min = mpi * (1.0 + 0.5 * mpi / M);
         c->ph_log_q02 = log(0.52544 / 0.06527);
         c->ph_inv_log_q02 = 1. / c->ph_log_q02;
+        c->ph_scale = 0.5 * 2.603096E-35 * c->scale_A;
     }
     { // dcs.hh:422, 435-436
         c->io_Wmin = 0.62 * I;

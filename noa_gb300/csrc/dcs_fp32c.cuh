@@ -441,38 +441,67 @@ NOA_HD double pprod_fp32c(double K, double q, const noa_dcs_consts &c, float &es
 }
 
 // ---------------------------------------------------------------- photonuclear
+// Float-pair constants of the photonuclear window: 2M, mpi, mpi^2, the ALLM
+// masses mP2 and mR2 (dcs.hh:262-288, 370-381), and 2M mpi + mpi^2.
+constexpr float kTwoMH = (float)(2. * PH_M), kTwoML = (float)(2. * PH_M - (double)kTwoMH);
+constexpr float kMpiH = (float)PH_MPI, kMpiL = (float)(PH_MPI - (double)kMpiH);
+constexpr float kMpi2H = (float)(PH_MPI * PH_MPI), kMpi2L = (float)(PH_MPI * PH_MPI - (double)kMpi2H);
+constexpr float kMP2H = (float)49.457, kMP2L = (float)(49.457 - (double)kMP2H);
+constexpr float kMR2H = (float)0.15052, kMR2L = (float)(0.15052 - (double)kMR2H);
+constexpr float kDConst = (float)(2. * PH_M * PH_MPI + PH_MPI * PH_MPI);
+
 // CHECKED = false: the caller has established that the pair is inside the
 // kinematic window; Q2min / Q2max are then formed in lean arithmetic.
 template <bool CHECKED = true>
 NOA_HD double photo_fp32c(double K, double q, const noa_dcs_consts &c, float &est) {
     est = 0.f;
     const double mass = c.mass;
-    const double E = K + mass;
-    double Q2min, Q2max;
+    // The window and its logs in float-float (~2^-44; FP64 only for E - q,
+    // whose q -> E edge float-float of E and q would not resolve).  Q2min =
+    // m^2 y^2 / (1 - y) = m^2 q^2 / (E (E - q)), Q2max = 2M (q - mpi) - mpi^2
+    // (dcs.hh:377-381); log Q2max - log Q2min as one log of their ratio.
+    FF Q2minF, Q2maxF;
+    const double Emq_d = (K + mass) - q;
+    const FF massF{c.mass_h, c.mass_l};
+    FF KF, qF;
     if (CHECKED) {
-        if (!photo_window(K, q, c, Q2min, Q2max))
+        double a, b;
+        if (!photo_window(K, q, c, a, b))
             return 0.;
+        Q2minF = ff_from(a);
+        Q2maxF = ff_from(b);
+        KF = ff_from(K);
+        qF = ff_from(q);
     } else {
-        const double yl = q * d_rcp(E);
-        Q2min = mass * mass * yl * yl * d_rcp((E - q) * d_rcp(E));
-        Q2max = 2.0 * PH_M * (q - PH_MPI) - PH_MPI * PH_MPI;
+        // the caller established the window (1 <= q < K); float-float holds
+        // q^2 and the window for K below 1e15, FP64 takes the rest
+        if (!(fpconv::f32(K) < 1e15f)) {
+            est = INFINITY;
+            return 0.;
+        }
+        KF = ff_split(K);
+        qF = ff_split(q);
     }
-    const double pQ2min = d_log(Q2min);
-    const double pQ2max = d_log(Q2max);
-    const double dpQ2 = pQ2max - pQ2min;
-    const double pQ2c = 0.5 * (pQ2max + pQ2min);
-    const double inv_E = d_rcp(E);
-    const float omy = fpconv::f32((E - q) * inv_E);  // 1 - y, kinematic edge q -> E
-    const float y = fpconv::f32(q * inv_E);
-    const double two_Mq_d = 2. * PH_M * q;
-    const float D = fpconv::f32(two_Mq_d - Q2max);  // 2Mq - Q2max = 2 M mpi + mpi^2 up to rounding
-    const float inv_2Mq = fpconv::f32(d_rcp(two_Mq_d));
+    const FF EF = ff_add(KF, massF);
+    const FF EmqF = ff_from(Emq_d);
+    if (!CHECKED) {
+        Q2minF = ff_div(ff_mul(ff_mul(massF, massF), ff_mul(qF, qF)), ff_mul(EF, EmqF));
+        Q2maxF = ff_add(ff_mul(FF{kTwoMH, kTwoML}, ff_add(qF, FF{-kMpiH, -kMpiL})), FF{-kMpi2H, -kMpi2L});
+    }
+    const FF dpQ2F = ff_log(ff_div(Q2maxF, Q2minF));
+    const FF pQ2cF = ff_add(ff_log(Q2minF), FF{0.5f * dpQ2F.h, 0.5f * dpQ2F.l});
+    const FF inv_EF = ff_div(FF{1.f, 0.f}, EF);
+    const float omy = ff_mul(EmqF, inv_EF).h;  // 1 - y, kinematic edge q -> E
+    const float y = ff_mul(qF, inv_EF).h;
+    const FF two_MqF = ff_mul(FF{kTwoMH, kTwoML}, qF);
+    const float D = kDConst;  // 2Mq - Q2max = 2 M mpi + mpi^2
+    const float inv_2Mq = ff_div(FF{1.f, 0.f}, two_MqF).h;
     const float inv_Mq = 2.f * inv_2Mq;
-    const float Q2maxf = fpconv::f32(Q2max);
-    const float half_dp = fpconv::f32(0.5 * dpQ2);
+    const float Q2maxf = Q2maxF.h;
+    const float half_dp = 0.5f * dpQ2F.h;
     // node abscissae log Q2 = pQ2c + (dpQ2 / 2) x_j in float-float
-    const float pc_h = fpconv::f32(pQ2c), pc_l = fpconv::f32(pQ2c - fpconv::f64(pc_h));
-    const float hd_h = half_dp, hd_l = fpconv::f32(0.5 * dpQ2 - fpconv::f64(hd_h));
+    const float pc_h = pQ2cF.h, pc_l = pQ2cF.l;
+    const float hd_h = half_dp, hd_l = 0.5f * dpQ2F.l;
 
     const float m02 = 0.31985f, mP2 = 49.457f, mR2 = 0.15052f;
     const float cP1 = 0.28067f, cP2 = 0.22291f, cP3 = 2.1979f;
@@ -481,13 +510,13 @@ NOA_HD double photo_fp32c(double K, double q, const noa_dcs_consts &c, float &es
     const float cR1 = 0.80107f, cR2 = 0.97307f, cR3 = 3.4942f;
     const float aR1 = 0.58400f, aR2 = 0.37888f, aR3 = 2.6063f;
     const float bR1 = 0.01147f, bR2 = 3.7582f, bR3 = 0.49338f;
-    const float inv_P = fpconv::f32(d_rcp(49.457 + two_Mq_d));
-    const float inv_R = fpconv::f32(d_rcp(0.15052 + two_Mq_d));
+    const float inv_P = ff_div(FF{1.f, 0.f}, ff_add(FF{kMP2H, kMP2L}, two_MqF)).h;
+    const float inv_R = ff_div(FF{1.f, 0.f}, ff_add(FF{kMR2H, kMR2L}, two_MqF)).h;
     const float inv_Q02 = 1.f / 0.52544f;
     const float inv_LQ = fpconv::f32(c.ph_inv_log_q02);
     const float Af = fpconv::f32(c.A), logA = fpconv::f32(c.ph_logA), a_low = fpconv::f32(c.ph_a_low);
-    const float two_m2 = fpconv::f32(2. * mass * mass);
-    const float invEE = fpconv::f32(inv_E * inv_E);
+    const float two_m2 = 2.f * c.mass2_f;
+    const float invEE = inv_EF.h * inv_EF.h;
     const float yy = y * y;
     KSum S;
     float err = 0.f;
@@ -554,8 +583,10 @@ NOA_HD double photo_fp32c(double K, double q, const noa_dcs_consts &c, float &es
     }
     const double ds_f = S.value();
     est = edge ? INFINITY : 0.6f * err * f_rcp(fpconv::f32(fabs(ds_f)));  // calibrated: max error <= est
-    const double ds = ds_f * 2.603096E-35 * d_rcp(q);
-    return (ds < 0.) ? 0. : 0.5 * ds * dpQ2 * (mass + K) * c.scale_A;
+    // 0.5 ds dpQ2 cf (m + K) / q N_A 1e3 / A (dcs.hh:402-404), cf = 2.603096e-35
+    const double fac = ff_to_double(ff_mul(dpQ2F, ff_div(ff_add(massF, KF), qF)));
+    const double ds = ds_f * fac;
+    return (ds < 0.) ? 0. : ds * c.ph_scale;
 }
 
 // ---------------------------------------------------------------- ionisation
