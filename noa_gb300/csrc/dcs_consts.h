@@ -46,6 +46,7 @@ typedef struct noa_dcs_consts {
     double br_BZ_e;         /* Z==1 ? 446   : 1429 Z^-2/3 */
     double br_D_n;          /* 1.54 A^0.27 */
     double br_dcs_factor;   /* 7.297182e-7 rem rem Z */
+    double br_scale;        /* br_dcs_factor scale_A (FP32C final scaling) */
     double br_half_m2;      /* 0.5 mass mass */
     double br_Dn_sqrte_m2;  /* D_n sqrte - 2 */
     double br_BZe_mass;     /* BZ_e mass */
@@ -117,6 +118,7 @@ static inline void noa_dcs_fill_consts(noa_dcs_consts *c, double A, double I, in
         c->br_BZ_e = (Z == 1) ? 446. : 1429. * pow((double)Z, -2. / 3.);
         c->br_D_n = 1.54 * pow(A, 0.27);
         c->br_dcs_factor = 7.297182E-07 * rem * rem * (double)Z;
+        c->br_scale = c->br_dcs_factor * c->scale_A;
         c->br_half_m2 = 0.5 * mass * mass;
         c->br_Dn_sqrte_m2 = c->br_D_n * sqrte - 2.;
         c->br_BZe_mass = c->br_BZ_e * mass;

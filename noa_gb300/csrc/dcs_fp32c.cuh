@@ -247,8 +247,8 @@ NOA_HD double brems_fp32c(double K, double q, const noa_dcs_consts &c, float &es
     if (!(S > 0.f) || !(Phi_n > 16.f * U32 || Phi_n < -16.f * U32) ||
         (below && !(Phi_e > 16.f * U32 || Phi_e < -16.f * U32)))
         est = INFINITY;
-    const double dcs = fpconv::f64(S * fac) * (c.br_dcs_factor * c.scale_A);
-    return (dcs < 0.) ? 0. : dcs;
+    const float sf = S * fac;
+    return (sf < 0.f) ? 0. : fpconv::f64(sf) * c.br_scale;  // br_scale > 0: the sign is sf's
 }
 
 // ---------------------------------------------------------------- pair production
@@ -605,7 +605,7 @@ constexpr float kTwoMeL = (float)(2. * ME - (double)kTwoMeH);
 // q = W_max as the reference writes it (dcs.hh:427-431); rearranged into
 // non-negative terms it runs in FP32, with W_max - q from the float-float
 // W_max (q >= 1e-5 below it, so to ~1e-8 relative).  The radiative
-// correction, a relative term of O(1e-2), is FP32, with E - q in FP64.
+// correction, a relative term of O(1e-2), is FP32, with E - q in float-float.
 NOA_HD double ion_fp32c(double K, double q, const noa_dcs_consts &c, float &est) {
     est = 0.f;
     const long long qb = dbits(q);
@@ -634,13 +634,15 @@ NOA_HD double ion_fp32c(double K, double q, const noa_dcs_consts &c, float &est)
     //   a0 + (a1 + a2/q)/q = 0.5/P2 + ((W_max - q)/(q W_max) + m^2/(P2 q))/q.
     const float iq = f_rcp(qf), iP2 = f_rcp(P2.h);
     const float bracket = 0.5f * iP2 + iq * (dW.h * iq * f_rcp(W.h) + c.mass2_f * iP2 * iq);
-    const double E = K + c.mass;
-    const float Ef = fpconv::f32(E);
+    // E and E - q in float-float (E - q >= m: no cancellation beyond E / m)
+    const FF EF = ff_add(Kx, FF{c.mass_h, c.mass_l});
+    const float Ef = EF.h;
     float cs = fpconv::f32(c.io_cZA) * Ef * bracket;
     float Delta = 0.f;
     if (dbits(K) >= dbits(c.io_k_rad)) {  // K >= k_rad, both positive
         const float L1 = log1pf(qf * (float)(2. / ME));
-        Delta = 1.16141E-03f * L1 * (logf(4.f * Ef * fpconv::f32(E - q) * fpconv::f32(c.inv_m2)) - L1);
+        const FF Emq = ff_add(EF, ff_neg(qx));
+        Delta = 1.16141E-03f * L1 * (logf(4.f * Ef * (Emq.h + Emq.l) * fpconv::f32(c.inv_m2)) - L1);
         cs *= 1.f + Delta;
     }
     // the close-collision term (max observed 8.7 u) and Delta relative to 1 + Delta
