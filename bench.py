@@ -519,9 +519,8 @@ def time_surrogate(torch, args):
         stats = {}
 
         def run():
-            o, st = sur.infer(tk, tq, counts)
+            _, st = sur.infer(tk, tq, counts, out=out)
             stats.update(st)
-            out.copy_(o)
         entry["surrogate_s"] = timed(run)
         nz = ref != 0
         rel = ((out[nz] - ref[nz]).abs() / ref[nz]).float()

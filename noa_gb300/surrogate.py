@@ -246,16 +246,20 @@ class Surrogate:
                 "heldout_frac_trusted": float(trust[cell[keep]].float().mean())}
 
     # ------------------------------------------------------------ inference
-    def infer(self, K, q, counts, tolerance=1e-6, trust=None):
+    def infer(self, K, q, counts, tolerance=1e-6, trust=None, out=None):
         """DCS of the pairs (K, q) (CUDA float64, segments of `counts` pairs,
         element i = elements_z[i]) through noa_dcs_mlp_infer: the network
-        (tcgen05) in trusted cells, the FP32C kernel elsewhere.  Returns
-        (result, {"network": n1, "fallback": n2, "status": st})."""
+        (tcgen05) in trusted cells, the FP32C kernel elsewhere.  Writes into
+        `out` when given (CUDA float64, K's size).  Returns (result,
+        {"network": n1, "fallback": n2, "status": st})."""
         trust = self.trust if trust is None else trust
         if trust is None:
             raise RuntimeError("no trust grid: call build_trust first")
-        tg = torch.as_tensor(np.ascontiguousarray(trust, dtype=np.uint8), device="cuda")
-        out = torch.empty_like(K)
+        tg = self._device_trust(trust)
+        if out is None:
+            out = torch.empty_like(K)
+        elif out.dtype != torch.float64 or not out.is_cuda or not out.is_contiguous() or out.numel() != K.numel():
+            raise RuntimeError("out must be a contiguous CUDA float64 tensor of K's size")
         n_seg = len(counts)
         els = (_lib.Element * n_seg)(*[_lib.element_struct(ELEMENTS[z]) for z in self.elements_z[:n_seg]])
         cnt = (ctypes.c_int64 * n_seg)(*[int(c) for c in counts])
@@ -267,6 +271,16 @@ class Surrogate:
             raise _lib.DcsError(st, lib.noa_dcs_mlp_infer_last_error().decode())
         torch.cuda.synchronize()
         return out, {"network": int(stats[0]), "fallback": int(stats[1]), "status": int(stats[2])}
+
+    def _device_trust(self, trust):
+        """The trust grid on the GPU, uploaded again only when it changes."""
+        host = np.ascontiguousarray(trust, dtype=np.uint8)
+        cached = getattr(self, "_trust_dev", None)
+        if cached is not None and cached[0].shape == host.shape and np.array_equal(cached[0], host):
+            return cached[1]
+        tg = torch.as_tensor(host, device="cuda")
+        self._trust_dev = (host.copy(), tg)
+        return tg
 
     def close(self):
         if getattr(self, "_h", None):

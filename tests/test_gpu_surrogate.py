@@ -79,6 +79,10 @@ def test_trusted_inference_within_bound(trained):
     assert st["network"] > 0.04 * nz.sum()
     assert float((rel > 1e-3).mean()) < 2e-3     # held-out-trusted cells generalise
     assert float(np.median(rel)) < 1e-4
+    # into a caller buffer: the same bits
+    buf = torch.full_like(tk, -7.0)
+    res, _ = s.infer(tk, tq, COUNTS, out=buf)
+    assert res is buf and torch.equal(buf, out)
 
 
 def test_untrusted_everywhere_is_the_fp32c_kernel(trained):
