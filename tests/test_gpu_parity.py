@@ -180,3 +180,40 @@ def test_large_size_properties(cuda_device, process):
     got = a.cpu().numpy()[idx]
     assert_fp64_parity(got, oracle.dcs(process, K[idx], q[idx], STANDARD_ROCK, MUON_MASS), "1e7 sample")
     assert np.all(np.isfinite(a.cpu().numpy()))
+
+
+@pytest.mark.parametrize("z", [1, 11, 82])
+@pytest.mark.parametrize("precision", ["fp64", "fp32c"])
+def test_pair_production_bounds(cuda_device, z, precision):
+    """Pair production decides q <= 4 me, q >= K + m (1 - 0.75 sqrt(e) Z^1/3)
+    and argmin >= 1 in float first, in float-float (K - q, argmin) where float
+    cannot, and in IEEE arithmetic within 1e-10 of a bound: pairs at relative
+    distances 1e-16..1e-2 on both sides of the two q bounds, and just above
+    q = 4 me where argmin -> 1, keep the reference's zero pattern and values."""
+    rng = np.random.default_rng(60 + z)
+    el = ELEMENTS[z] if z != 11 else STANDARD_ROCK
+    me, m = 0.510998910e-03, MUON_MASS
+    z13 = float(el.Z) ** (1.0 / 3.0)
+    shift = m * (1.0 - 0.75 * np.sqrt(np.e) * z13)
+    n = 200_000
+    K = 10 ** rng.uniform(-2, 9, n)
+    side = rng.choice([-1.0, 1.0], n)
+    rel = 10 ** rng.uniform(-16, -2, n)
+    q1 = 4 * me * (1 + side * rel)
+    q2 = (K + shift) * (1 + side * rel)
+    q3 = 4 * me * (1 + 10 ** rng.uniform(-12, 0, n))
+    for q in (q1, q2, q3):
+        got = gpu_dcs(1, K, q, el, MUON_MASS, precision)
+        exp = oracle.dcs(1, K, q, el, MUON_MASS)
+        s = rel_stats(got, exp)
+        assert s["zero_agree"] and s["nonfinite_agree"], s
+        # values relative to the reference's own conditioning: near these
+        # edges a 4e-16 change of K and q moves its output by up to ~40%
+        nz = exp != 0
+        sens = np.zeros_like(exp)
+        for d in (4e-16, -4e-16):
+            o = oracle.dcs(1, K * (1 + d), q * (1 - d), el, MUON_MASS)
+            sens[nz] = np.maximum(sens[nz], np.abs(o[nz] - exp[nz]) / exp[nz])
+        err = np.abs(got[nz] - exp[nz]) / exp[nz]
+        floor = 1e-12 if precision == "fp64" else 1e-6
+        assert np.all(err <= 64 * sens[nz] + floor), float((err - 64 * sens[nz]).max())
