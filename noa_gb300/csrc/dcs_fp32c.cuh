@@ -1,13 +1,15 @@
 /*
  * FP32-compensated ("FP32C") forms of the four muon DCS processes.
  *
- * The quadrature bodies run in FP32, with compensated node sums.  FP64 is
- * kept where float would lose the answer: the kinematic bounds (decided
- * exactly as the reference decides them, so the zero pattern is the
- * reference's), the kinematic-edge differences E - q, 1 - nu, 2Mq - Q2 and
- * the node arguments t tmin / log Q2 (formed in double, then split into a
- * float pair), the kinematic-limit logs log(argmin), log Q2min, log Q2max,
- * and the final macroscopic scaling (its constants are far below FLT_MIN).
+ * The quadrature bodies run in FP32, with compensated node sums.  Where
+ * float would lose the answer the arithmetic is float-float (FF, ~2^-44 on
+ * the FP32 pipe) or FP64: the kinematic bounds are decided in float with a
+ * margin and exactly (FP64 / FF) inside it, so the zero pattern is the
+ * reference's; the kinematic-edge differences E - q (FP64), 1 - nu and
+ * 2Mq - Q2; the node arguments t tmin and log Q2 as float pairs; the
+ * kinematic-limit logs log(argmin), log Q2min and log(Q2max / Q2min) in FF;
+ * and the final macroscopic scaling in double (its constants are far below
+ * FLT_MIN).
  *
  * Reformulations that remove float cancellations, all exact algebra:
  *  - pair production Be / Bmu, dcs.hh:188-216: the terms
@@ -25,7 +27,8 @@
  * float rounding error (a few units of 2^-24 per operation, scaled by the size
  * of what cancels), or infinity where a branch or clamp of the reference sits
  * within rounding distance.  When est exceeds the caller's tolerance the
- * kernel evaluates that pair in FP64 instead.
+ * kernel evaluates that pair in FP64 instead (pair production: first again
+ * in FP32 with its screening log in FF, pprod_fp32c<false, true>).
  *
  * Written for host and device (NOA_HD) so that the same source can be
  * checked against the CPU oracle.
