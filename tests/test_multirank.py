@@ -33,7 +33,7 @@ def _rank(rank, world, port, n, out):
 
 def test_two_gloo_ranks_shard_and_reduce():
     n, world = 2000, 2
-    with mp.Manager() as m:
+    with mp.get_context("spawn").Manager() as m:  # no fork of a multi-threaded process
         out = m.dict()
         mp.spawn(_rank, args=(world, _free_port(), n, out), nprocs=world, join=True)
         res = dict(out)
