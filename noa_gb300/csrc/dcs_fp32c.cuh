@@ -223,14 +223,25 @@ NOA_HD FF ff_log(FF x) {
 // ---------------------------------------------------------------- bremsstrahlung
 NOA_HD double brems_fp32c(double K, double q, const noa_dcs_consts &c, float &est) {
     est = 0.f;
-    const double E = K + c.mass;
-    const float Ef = fpconv::f32(E), qf = fpconv::f32(q);
+    const float Kf = fpconv::f32(K), qf = fpconv::f32(q);
+    if (!(Kf > 1e-20f && Kf < 1e30f && qf > 1e-20f && qf < 1e30f)) {  // NaN, q <= 0, extreme ranges: FP64
+        est = INFINITY;
+        return 0.;
+    }
+    // E = K + m and E - q in float-float; q within 1e-4 of E (or above it),
+    // where that difference would lose digits, goes to FP64
+    const FF EF = ff_add(ff_split(K), FF{c.mass_h, c.mass_l});
+    const FF EmqF = ff_add(EF, ff_neg(ff_split(q)));
+    const float Ef = EF.h, Emq = EmqF.h + EmqF.l;
+    if (!(Emq > 1e-4f * Ef)) {
+        est = INFINITY;
+        return 0.;
+    }
     // q < qe_max (physics.hh:142): float decision, exact when close
     const float qe = f_div(Ef, 1.f + fpconv::f32(c.br_half_m2) * f_rcp((float)ME * Ef));
     bool below = qf < qe;
     if (fabsf(qf - qe) <= 1e-5f * qe)
-        below = brems_below_qe(E, q, c);
-    const float Emq = fpconv::f32(E - q);
+        below = brems_below_qe(K + c.mass, q, c);
     const float sqrte = 1.648721271f;
     // delta = 0.5 m^2 nu / (E (1 - nu)) = 0.5 m^2 q / (E (E - q))
     const float delta = fpconv::f32(c.br_half_m2) * qf * f_rcp(Ef * Emq);

@@ -107,6 +107,7 @@ __global__ void __launch_bounds__(CL_THREADS) classify_kernel(const __grid_const
     __shared__ uint8_t s_seg[CL_ITEMS][CL_THREADS];
     const int64_t n = p.seg_begin[p.n_seg];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    int seg_at = 0;  // segment of this thread's last pair
     for (int64_t tile = (int64_t)blockIdx.x * CL_THREADS * CL_ITEMS; tile < n;
          tile += (int64_t)gridDim.x * CL_THREADS * CL_ITEMS) {
         unsigned net_mask = 0, fb_mask = 0;
@@ -114,10 +115,12 @@ __global__ void __launch_bounds__(CL_THREADS) classify_kernel(const __grid_const
         for (int j = 0; j < CL_ITEMS; j++) {
             const int64_t i = tile + j * CL_THREADS + threadIdx.x;
             float4 f = make_float4(0.f, 0.f, 0.f, 0.f);
-            int seg = 0;
+            int seg = seg_at;
             if (i < n) {
+                // a thread's pairs come in increasing order: resume the search
                 while (seg + 1 < p.n_seg && i >= p.seg_begin[seg + 1])
                     seg++;
+                seg_at = seg;
                 const noa_dcs_consts &c = p.consts[seg];
                 const double K = p.K[i], q = p.q[i];
                 const bool open = open_fast<PROC>(K, q, c);
