@@ -94,7 +94,7 @@ __device__ __forceinline__ double brems_fp64(double K, double q, const noa_dcs_c
 // to the constants would copy them to local memory).
 static __device__ __noinline__ bool pprod_live_tail(double K, double q, double mass, float inv_mass_h, float inv_mass_l,
                                              float x0) {
-    noa_dcs_consts c;
+    noa_dcs_consts c;  // pprod_argmin_ff / _exact read only these three fields
     c.mass = mass;
     c.inv_mass_h = inv_mass_h;
     c.inv_mass_l = inv_mass_l;
