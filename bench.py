@@ -3,23 +3,29 @@
 
 Workload (one "step"): the four DCS processes of NOA's PMS module --
 bremsstrahlung, pair production, photonuclear, ionisation -- evaluated in
-plain FP64 over 1e7 seeded (K, q) pairs of standard rock for a muon, i.e.
-4e7 DCS evaluations.  This is the reference's benchmark of
+plain FP64 over 1e8 seeded (K, q) pairs of standard rock for a muon, i.e.
+4e8 DCS evaluations.  This is the reference's benchmark of
 benchmark/measure-dcs-calc.cc (vectorised dcs::vmap per process) at the
-1e7-pair configuration; the pairs follow K ~ log-uniform[1e-3, 1e6] GeV,
-nu ~ log-uniform[1e-7, 1], q = nu K (noa_gb300.workload, seed 987654).
+mixed-precision target size of 1e8 pairs; the pairs follow
+K ~ log-uniform[1e-3, 1e6] GeV, nu ~ log-uniform[1e-7, 1], q = nu K
+(noa_gb300.workload, seed 987654).
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 
 `value` is DCS evaluations per second with inputs resident in HBM (CUDA
-events on the launching stream; K and q are 160 MB, above the 129 MB L2, so
-no flush is needed between steps).  `e2e` is the same metric through the C
+events on the launching stream; K and q are 1.6 GB, far above the 129 MB L2,
+so no flush is needed between steps).  `e2e` is the same metric through the C
 ABI's host-buffer entry point (noa_dcs_vmap_host) from pinned host memory,
 host-device traffic included: the kernels read K and q and write the results
-in the page-locked host buffers over NVLink-C2C.  `--impl reference` times
-the reference algorithm on the host cores instead (the CPU oracle, an
-operation-for-operation restatement of src/noa/pms/dcs.hh, OpenMP over all
-cores like dcs::pvmap).
+in the page-locked host buffers over NVLink-C2C.  Beside it, on the same
+pairs: the FP32-compensated form, the reference's own CUDA bremsstrahlung
+kernel (src/noa/pms/dcs.cuh, compiled unmodified for sm_103a by
+oracle/build_ref.sh), the batched multi-element engine, the learned
+surrogate, and the per-K integrals.  `--impl reference` times the reference's
+CPU implementation on the host cores: its own dcs::pvmap (src/noa/pms/dcs.hh,
+OpenMP over all cores) where oracle/build_ref.sh compiled it, else the CPU
+oracle (an operation-for-operation restatement, bit-exact with it).  The
+line ends with a compact `summary` of all of these.
 """
 import argparse
 import json
@@ -37,7 +43,7 @@ sys.path.insert(0, ROOT)
 
 METRIC = "DCS evals/sec per process on 1 GB300 (plain FP64 vs FP32-comp vs MLP) at stated rel. error"
 PROCESSES = ("bremsstrahlung", "pair_production", "photonuclear", "ionisation")
-N_PAIRS = 10_000_000
+N_PAIRS = 100_000_000
 # Algorithmic work per evaluation on this workload, in flop-equivalents
 # (+ - * / sqrt compare = 1, log exp pow log10 = 20), counted by running the
 # reference's operation sequence on an op-counting scalar over 1e6 pairs of
@@ -57,7 +63,7 @@ def parse_args():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-batched", action="store_true")
-    ap.add_argument("--no-mixed-1e8", action="store_true")
+    ap.add_argument("--no-reference-cuda", action="store_true")
     ap.add_argument("--no-integrals", action="store_true")
     ap.add_argument("--no-surrogate", action="store_true")
     ap.add_argument("--surrogate-queries", type=int, default=100_000_000)
@@ -87,24 +93,48 @@ def reduce_max(value, world, device=None):
 
 
 # ---------------------------------------------------------------- CPU side
-def cpu_reference_rate(n_sample, reps=5, offset=0, threads=0):
-    """Evaluations/s of the oracle (reference algorithm) on the first
-    n_sample pairs of the workload, all four processes, median of reps runs
-    after one warm-up; threads 0 = every host thread (dcs::pvmap), 1 = the
-    serial loop (dcs::vmap)."""
+def cpu_dcs_fn():
+    """The CPU implementation timed as the baseline: the reference's own
+    dcs::pvmap / dcs::vmap (oracle/_ref/libnoa_ref_dcs_bench.so, compiled from
+    src/noa/pms/dcs.hh by oracle/build_ref.sh with the reference benchmark's
+    flags: -O3, OpenMP) where it was built on this host, else the oracle port.  Returns (fn, kind) with
+    fn(process, K, q, threads) -> out; threads 0 = every host thread
+    (dcs::pvmap), 1 = the serial loop (dcs::vmap)."""
     import oracle
     from noa_gb300.elements import MUON_MASS, STANDARD_ROCK
+    if oracle.ref_available("bench"):
+        try:
+            oracle.ref_lib("bench")
+
+            def fn(p, K, q, threads):
+                return oracle.ref_dcs(p, K, q, STANDARD_ROCK, MUON_MASS, parallel=threads != 1, build="bench")
+            return fn, "reference"
+        except OSError:
+            pass
+
+    def port(p, K, q, threads):
+        return oracle.dcs(p, K, q, STANDARD_ROCK, MUON_MASS, threads=threads)
+    return port, "port"
+
+
+def cpu_reference_rate(n_sample, reps=5, offset=0, threads=0):
+    """Evaluations/s of the CPU baseline (cpu_dcs_fn) on the first n_sample
+    pairs of the workload, all four processes, median of reps runs after one
+    warm-up; threads 0 = every host thread (dcs::pvmap), 1 = the serial loop
+    (dcs::vmap)."""
+    import oracle
     from noa_gb300.workload import kinetic_recoil
+    fn, kind = cpu_dcs_fn()
     K, q = kinetic_recoil(n_sample, offset=offset)
     for p in range(4):
-        oracle.dcs(p, K, q, STANDARD_ROCK, MUON_MASS, threads=threads)
+        fn(p, K, q, threads)
     per = {}
     total_t = []
     for _ in range(reps):
         t_all = 0.0
         for p, name in enumerate(PROCESSES):
             t0 = time.perf_counter()
-            oracle.dcs(p, K, q, STANDARD_ROCK, MUON_MASS, threads=threads)
+            fn(p, K, q, threads)
             dt = time.perf_counter() - t0
             per.setdefault(name, []).append(dt)
             t_all += dt
@@ -115,6 +145,7 @@ def cpu_reference_rate(n_sample, reps=5, offset=0, threads=0):
         "seconds_per_sample": t,
         "per_process": {k: n_sample / statistics.median(v) for k, v in per.items()},
         "cores": oracle.lib().oracle_max_threads() if threads == 0 else threads,
+        "kind": kind,
     }
 
 
@@ -124,22 +155,25 @@ def run_reference(args):
         return
     n_sample = min(args.n, 2_000_000)
     import oracle
-    from noa_gb300.elements import MUON_MASS, STANDARD_ROCK
     from noa_gb300.workload import kinetic_recoil
+    fn, kind = cpu_dcs_fn()
     K, q = kinetic_recoil(n_sample)
     for _ in range(args.warmup):
         for p in range(4):
-            oracle.dcs(p, K, q, STANDARD_ROCK, MUON_MASS, threads=0)
+            fn(p, K, q, 0)
     times = []
     for _ in range(args.steps):
         t0 = time.perf_counter()
         for p in range(4):
-            oracle.dcs(p, K, q, STANDARD_ROCK, MUON_MASS, threads=0)
+            fn(p, K, q, 0)
         times.append(time.perf_counter() - t0)
     total = sum(times)
     value = 4 * n_sample * args.steps / total
     cores = oracle.lib().oracle_max_threads()
-    sample = (f"first {n_sample} pairs of the 1e7-pair workload per step, all four processes "
+    what = ("the reference's own dcs::pvmap (src/noa/pms/dcs.hh compiled on this host with its benchmark's "
+            "flags, -O3 -fopenmp)"
+            if kind == "reference" else "the CPU oracle port of dcs::pvmap (OpenMP)")
+    sample = (f"{what}: first {n_sample} pairs of the {args.n:.0e}-pair workload per step, all four processes "
               f"(the pairs are i.i.d., so the rate is the workload's)")
     line = {
         "metric": METRIC, "value": value, "unit": "evals/s", "impl": "reference", "n_gpus": args.gpus,
@@ -147,7 +181,7 @@ def run_reference(args):
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic: seeded log-uniform K in [1e-3,1e6] GeV, nu in [1e-7,1], q = nu K",
         "config": config_dict(args.n, world),
-        "cpu_baseline": {"value": value, "unit": "evals/s", "cores": cores, "kind": "port", "sample": sample},
+        "cpu_baseline": {"value": value, "unit": "evals/s", "cores": cores, "kind": kind, "sample": sample},
         "e2e": {"value": value, "unit": "evals/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -158,7 +192,8 @@ def config_dict(n, world):
             "n_pairs_per_gpu": n, "processes": list(PROCESSES),
             "element": {"A": 22.0, "I": 0.1364e-6, "Z": 11}, "mass": 0.10565839,
             "parallelism": f"replicas x{world} (independent shards)" if world > 1 else "single GPU",
-            "l2": "inputs 160 MB > 129 MB L2: no flush between steps"}
+            "l2": f"inputs {16 * n / 1e9:.3g} GB vs 129 MB L2: "
+                  + ("no flush between steps" if 16 * n > 129e6 else "smaller than L2")}
 
 
 # ---------------------------------------------------------------- clocks
@@ -218,9 +253,12 @@ class ClockSampler:
 
 
 # ---------------------------------------------------------------- GPU side
-def measure_fp64_peak(lib, torch, stream):
-    """FP64 FMA-chain throughput (TFLOP/s) of this GPU: the roofline denominator."""
+def measure_fp64_peak(torch, stream):
+    """FP64 FMA-chain throughput (TFLOP/s) of this GPU: the roofline
+    denominator (probe of the instrument library libnoa_dcs_diag.so)."""
     import ctypes
+    from noa_gb300 import _lib
+    lib = _lib.load_diag()
     sms = torch.cuda.get_device_properties(0).multi_processor_count
     blocks = sms * 8
     out = torch.empty(blocks * 256, dtype=torch.float64, device="cuda")
@@ -278,60 +316,62 @@ def time_fp32c(lib, torch, tk, tq, ref_outs, n, el, mass, stream, args, fp64_s):
     return res
 
 
-def time_mixed_1e8(torch, args):
-    """The mixed-precision target workload: 1e8 seeded pairs of standard rock,
-    each process in plain FP64 and in FP32C (tolerance 1e-6) on the same
-    pairs: ms per launch, speed-up, the FP32C error against FP64, and the
-    FP64 output against the oracle on a seeded sample of 1e5 of the pairs."""
-    from noa_gb300 import _lib
-    from noa_gb300.elements import MUON_MASS, STANDARD_ROCK
-    from noa_gb300.workload import kinetic_recoil
-    import numpy as np
+def time_reference_cuda(torch, tk, tq, ours, n, args, sample_idx):
+    """The reference's own CUDA kernel, dcs::cuda::vmap_bremsstrahlung
+    (src/noa/pms/dcs.cuh:30-41: one thread per pair, legacy default stream),
+    compiled unmodified for sm_103a by oracle/build_ref.sh, timed with CUDA
+    events on the default stream over the same device-resident pairs as the
+    headline; its output is compared with this repository's bremsstrahlung
+    over all pairs and with the oracle on the parity sample."""
     import oracle
-    n = 100_000_000
-    K, q = kinetic_recoil(n, offset=1 << 33)
-    tk, tq = torch.from_numpy(K).cuda(), torch.from_numpy(q).cuda()
-    idx = np.sort(np.random.default_rng(7).choice(n, 100_000, replace=False))
-    Ks, qs = K[idx], q[idx]
-    del K, q
-    o64, o32 = torch.empty_like(tk), torch.empty_like(tk)
-    lib = _lib.load()
-    el = _lib.element_struct(STANDARD_ROCK)
-    stream = torch.cuda.current_stream()
-    res = {"n_pairs": n, "element": "standard rock", "tolerance": 1e-6}
-    reps = max(1, min(args.steps, 2))
-    tot64 = tot32 = 0.0
-    for p, name in enumerate(PROCESSES):
-        ms = {}
-        for prec, out in ((0, o64), (1, o32)):
-            def launch():
-                _lib.check(lib.noa_dcs_cuda_vmap(p, prec, out.data_ptr(), tk.data_ptr(), tq.data_ptr(), n, el,
-                                                 MUON_MASS, stream.cuda_stream))
-            launch()
-            s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-            torch.cuda.synchronize()
-            s.record(stream)
-            for _ in range(reps):
-                launch()
-            e.record(stream)
-            torch.cuda.synchronize()
-            ms[prec] = s.elapsed_time(e) / reps
-        tot64 += ms[0]
-        tot32 += ms[1]
-        # the FP64 output against the oracle on a seeded sample of the 1e8 pairs
-        ref = oracle.dcs(p, Ks, qs, STANDARD_ROCK, MUON_MASS)
-        got = o64[torch.from_numpy(idx).to(o64.device)].cpu().numpy()
-        nz = ref != 0
-        rel = np.abs(got[nz] - ref[nz]) / np.abs(ref[nz]) if nz.any() else np.zeros(1)
-        res[name] = {"fp64_ms": ms[0], "fp32c_ms": ms[1], "speedup": ms[0] / ms[1],
-                     "fp32c_evals_per_s": n / (ms[1] * 1e-3), **rel_error_stats(torch, o32, o64),
-                     "fp64_vs_oracle_sample": {"mean_rel": float(rel.mean()), "max_rel": float(rel.max()),
-                                               "zero_pattern_equal": bool(np.array_equal(got == 0, ref == 0))}}
-    res["all_processes"] = {"fp64_evals_per_s": 4 * n / (tot64 * 1e-3), "fp32c_evals_per_s": 4 * n / (tot32 * 1e-3),
-                            "speedup": tot64 / tot32}
-    del tk, tq, o64, o32
-    torch.cuda.empty_cache()
+    from noa_gb300.elements import MUON_MASS, STANDARD_ROCK
+    if not oracle.ref_cuda_available():
+        return {"available": False,
+                "why": "oracle/_ref/libnoa_ref_cuda.so not built (no noa checkout or staged headers at build time)"}
+    out = torch.empty_like(tk)
+    stream = torch.cuda.default_stream()
+
+    def launch():
+        oracle.ref_cuda_bremsstrahlung(out.data_ptr(), tk.data_ptr(), tq.data_ptr(), n, STANDARD_ROCK, MUON_MASS)
+
+    torch.cuda.synchronize()
+    for _ in range(max(1, args.warmup)):
+        launch()
+    steps = max(1, min(args.steps, 5))
+    s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    s.record(stream)
+    for _ in range(steps):
+        launch()
+    e.record(stream)
+    torch.cuda.synchronize()
+    ms = s.elapsed_time(e) / steps
+    res = {"available": True, "ms_per_launch": ms, "evals_per_s": n / (ms * 1e-3),
+           "vs_ours": rel_error_stats(torch, out, ours)}
+    ref = oracle.dcs(0, *sample_idx[1:], STANDARD_ROCK, MUON_MASS)
+    got = out[torch.from_numpy(sample_idx[0]).to(out.device)].cpu().numpy()
+    nz = ref != 0
+    rel = np.abs(got[nz] - ref[nz]) / np.abs(ref[nz])
+    res["vs_oracle_sample"] = {"mean_rel": float(rel.mean()), "max_rel": float(rel.max())}
+    del out
     return res
+
+
+def conditioning_ratio(p, K, q, got, ref, element, mass, delta=4e-16):
+    """Largest ratio of a point's relative error to 64 x the reference's own
+    response to +-delta relative changes of K and q, plus 1e-12 (the per-point
+    parity bar of the tests); <= 1 means every point is within it."""
+    import oracle
+    ok = np.isfinite(ref) & (ref != 0)
+    sens = np.zeros_like(ref)
+    for dk in (delta, -delta):
+        for dq in (delta, -delta):
+            o = oracle.dcs(p, K * (1 + dk), q * (1 + dq), element, mass)
+            with np.errstate(invalid="ignore", divide="ignore", over="ignore"):
+                r = np.abs(o - ref) / np.abs(ref)
+            sens = np.maximum(sens, np.where(ok & np.isfinite(r), r, np.where(ok, np.inf, 0.0)))
+    err = np.abs(got[ok] - ref[ok]) / np.abs(ref[ok])
+    return float(np.max(err / (64 * sens[ok] + 1e-12))) if ok.any() else 0.0
 
 
 def time_batched(torch, args):
@@ -607,11 +647,15 @@ def run_ours(args):
     value = world * 4 * n * args.steps / elapsed
 
     # parity of the timed outputs: a seeded sample of 1e5 pairs against the
-    # oracle (the reference's algorithm, bit-exact with it on the CPU)
+    # oracle (the reference's algorithm, bit-exact with it on the CPU): the
+    # reference's mean metric, the max, the zero pattern, and the per-point
+    # conditioning bar of the tests (cond_ratio <= 1)
     parity = None
+    sample = None
     if rank == 0:
         import oracle
         idx = np.sort(np.random.default_rng(2024).choice(n, min(n, 100_000), replace=False))
+        sample = (idx, K[idx], q[idx])
         ti = torch.from_numpy(idx).to(dev)
         parity = {"sample": f"{len(idx)} seeded indices of the timed step's pairs"}
         for p, name in enumerate(PROCESSES):
@@ -620,7 +664,9 @@ def run_ours(args):
             nz = ref != 0
             rel = np.abs(got[nz] - ref[nz]) / np.abs(ref[nz]) if nz.any() else np.zeros(1)
             parity[name] = {"mean_rel": float(rel.mean()), "max_rel": float(rel.max()),
-                            "zero_pattern_equal": bool(np.array_equal(got == 0, ref == 0))}
+                            "zero_pattern_equal": bool(np.array_equal(got == 0, ref == 0)),
+                            "cond_ratio": conditioning_ratio(p, K[idx], q[idx], got, ref, STANDARD_ROCK,
+                                                             MUON_MASS)}
 
     # e2e: host buffers in pinned memory, through noa_dcs_vmap_host, host-device traffic timed.
     e2e = None
@@ -649,6 +695,7 @@ def run_ours(args):
         for p in range(4):
             if not torch.equal(hout[p], outs[p].cpu()):
                 raise RuntimeError(f"e2e result differs from device result for {PROCESSES[p]}")
+        del hk, hq, hout
 
     variants = {"fp64": {name: {"evals_per_s": n * args.steps / t} for name, t in per_proc_s.items()}}
     variants["fp32c"] = time_fp32c(lib, torch, tk, tq, outs, n, el, MUON_MASS, stream, args, per_proc_s)
@@ -658,11 +705,23 @@ def run_ours(args):
             tdist.destroy_process_group()
         return
 
-    peak = measure_fp64_peak(lib, torch, stream)
+    ref_cuda = None
+    if not args.no_reference_cuda:
+        ref_cuda = time_reference_cuda(torch, tk, tq, outs[0], n, args, sample)
+        if ref_cuda.get("available"):
+            ref_cuda["ours_ms_per_launch"] = 1e3 * per_proc_s["bremsstrahlung"] / args.steps
+            ref_cuda["speedup_of_ours"] = ref_cuda["ms_per_launch"] / ref_cuda["ours_ms_per_launch"]
+    del tk, tq, outs
+    torch.cuda.empty_cache()
+
+    peak = measure_fp64_peak(torch, stream)
     dom = max(per_proc_s, key=per_proc_s.get)
     dom_launch_s = per_proc_s[dom] / args.steps
     achieved = FLOP_EQ_PER_EVAL[dom] * n / dom_launch_s / 1e12
-    traffic = load_traffic().get(f"{dom}_fp64_1e7")
+    # ncu DRAM bytes of one 1e7-pair launch, scaled to this launch's pairs
+    # (the kernels read and write every pair once, so traffic grows in proportion)
+    t7 = load_traffic().get(f"{dom}_fp64_1e7")
+    traffic = t7 * n / 1e7 if t7 else None
     per_process = {name: {"evals_per_s": n * args.steps / t, "ms_per_launch": 1e3 * t / args.steps,
                           "flop_eq_tflops": FLOP_EQ_PER_EVAL[name] * n * args.steps / t / 1e12,
                           "hbm_gbs": BYTES_PER_EVAL * n * args.steps / t / 1e9}
@@ -676,7 +735,10 @@ def run_ours(args):
         "roofline": {"bound": "fp64", "kernel": f"{dom} FP64", "achieved": achieved, "peak": peak,
                      "unit": "TFLOP/s", "frac": achieved / peak if peak else None,
                      "traffic": traffic,
-                     "peak_source": "FP64 FMA-chain probe (noa_dcs_probe_fma) measured in this run",
+                     "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of a 1e7-pair launch "
+                                       "(profiles/traffic.json) x n / 1e7",
+                     "peak_source": "FP64 FMA-chain probe (noa_dcs_probe_fma, libnoa_dcs_diag.so) measured in "
+                                    "this run",
                      "numerator": f"{FLOP_EQ_PER_EVAL[dom]} flop-eq/eval x {n} evals per launch"},
         "per_process": per_process,
         "variants": variants,
@@ -686,8 +748,8 @@ def run_ours(args):
     }
     if parity is not None:
         line["parity_vs_oracle"] = parity
-    if not args.no_mixed_1e8 and world == 1:
-        line["mixed_precision_1e8"] = time_mixed_1e8(torch, args)
+    if ref_cuda is not None:
+        line["reference_cuda_bremsstrahlung"] = ref_cuda
     if not args.no_batched:
         line["batched"] = time_batched(torch, args)
     if not args.no_integrals:
@@ -698,15 +760,65 @@ def run_ours(args):
     if not args.no_cpu_baseline and world == 1:
         cb = cpu_reference_rate(min(n, 1_000_000))
         c1 = cpu_reference_rate(min(n, 100_000), reps=3, threads=1)
-        line["cpu_baseline"] = {"value": cb["value"], "unit": "evals/s", "cores": cb["cores"], "kind": "port",
-                                "sample": "first 1e6 pairs of the workload, all four processes, median of 5 "
-                                          "after a warm-up",
+        what = ("the reference's own dcs::pvmap (src/noa/pms/dcs.hh compiled on this host with its benchmark's "
+                "flags, -O3 -fopenmp)"
+                if cb["kind"] == "reference" else "the CPU oracle port of dcs::pvmap (OpenMP)")
+        line["cpu_baseline"] = {"value": cb["value"], "unit": "evals/s", "cores": cb["cores"], "kind": cb["kind"],
+                                "sample": f"{what}: first 1e6 pairs of the workload, all four processes, "
+                                          "median of 5 after a warm-up",
                                 "per_process": cb["per_process"],
                                 "single_thread": {"value": c1["value"], "per_process": c1["per_process"],
-                                                  "sample": "first 1e5 pairs, median of 3"}}
+                                                  "sample": "dcs::vmap, first 1e5 pairs, median of 3"}}
+    line["summary"] = summarise(line)
     print(json.dumps(line), flush=True)
     if world > 1:
         tdist.destroy_process_group()
+
+
+def _r(x, d=4):
+    """x rounded to d significant digits (None passes through)."""
+    if x is None:
+        return None
+    return float(f"{x:.{d}g}")
+
+
+def summarise(line):
+    """A compact digest of the whole line, printed last so that a reader
+    keeping only the end of the line still has every headline figure."""
+    s = {"workload": line["config"]["workload"], "fp64_evals_per_s": _r(line["value"]),
+         "e2e_evals_per_s": _r((line.get("e2e") or {}).get("value")),
+         "roofline_frac": _r(line["roofline"]["frac"], 3)}
+    par = line.get("parity_vs_oracle")
+    if par:
+        s["fp64_vs_oracle"] = {k: {"mean": _r(v["mean_rel"], 2), "max": _r(v["max_rel"], 2),
+                                   "cond_ratio": _r(v["cond_ratio"], 2), "zeros_equal": v["zero_pattern_equal"]}
+                               for k, v in par.items() if isinstance(v, dict)}
+    f = line["variants"].get("fp32c")
+    if f:
+        s["fp32c"] = {k: {"x_fp64": _r(v["speedup_vs_fp64"], 3), "max": _r(v["max_rel"], 2),
+                          "median": _r(v["median_rel"], 2)} for k, v in f.items() if k in PROCESSES}
+        s["fp32c"]["all"] = {"x_fp64": _r(f["all_processes"]["speedup_vs_fp64"], 3),
+                             "evals_per_s": _r(f["all_processes"]["evals_per_s"])}
+    rc = line.get("reference_cuda_bremsstrahlung")
+    if rc:
+        s["reference_cuda_brems"] = ({"ms": _r(rc["ms_per_launch"]), "ours_ms": _r(rc["ours_ms_per_launch"]),
+                                      "x": _r(rc["speedup_of_ours"], 3),
+                                      "mean_vs_ours": _r(rc["vs_ours"]["mean_rel"], 2)}
+                                     if rc.get("available") else "unavailable")
+    b = line.get("batched")
+    if b:
+        s["batched_evals_per_s"] = {p: _r(b[p]["all_processes"]["evals_per_s"]) for p in ("fp64", "fp32c")}
+    sg = line.get("surrogate")
+    if sg:
+        s["surrogate"] = {k: {"x_fp64": _r(v["speedup_vs_fp64"], 3), "x_fp32c": _r(v["speedup_vs_fp32c"], 3),
+                              "max": _r(v["max_rel"], 2), "above_1e-3": v["frac_above_1e-3"],
+                              "net_share": _r(v["network_share_of_open"], 2),
+                              "train_s": _r(v["training"].get("train_seconds"), 3)}
+                          for k, v in sg.items() if isinstance(v, dict) and "speedup_vs_fp64" in v}
+    cb = line.get("cpu_baseline")
+    if cb:
+        s["cpu_baseline"] = {"evals_per_s": _r(cb["value"]), "kind": cb["kind"], "cores": cb["cores"]}
+    return s
 
 
 def main():

@@ -60,8 +60,6 @@ SIGNATURES = {
     "noa_dcs_status_string": (ctypes.c_char_p, [_INT]),
     "noa_dcs_last_error": (ctypes.c_char_p, []),
     "noa_dcs_abi_version": (_INT, []),
-    "noa_dcs_probe_fma": (_INT, [_INT, _P, _INT, _INT, ctypes.POINTER(_D), _P]),
-    "noa_dcs_lean64_eval": (_INT, [_INT, _P, _P, _P, _I64, _P]),
     "noa_dcs_batch_plan_create": (_INT, [ctypes.POINTER(_P), _INT, _INT, _INT, _EP, ctypes.POINTER(_I64), _D]),
     "noa_dcs_batch_plan_set_tile": (_INT, [_P, _INT, _INT, _INT]),
     "noa_dcs_batch_plan_get_tile": (_INT, [_P, ctypes.POINTER(_INT), ctypes.POINTER(_INT), ctypes.POINTER(_INT)]),
@@ -86,7 +84,15 @@ SIGNATURES = {
     "noa_dcs_cuda_vmap_batched_noalloc": (_INT, [_INT, _INT, _INT, _EP, ctypes.POINTER(_I64), _D, _P, _P, _P, _P]),
 }
 
+# Test and bench instruments, noa_gb300/libnoa_dcs_diag.so (csrc/diag/noa_dcs_diag.h).
+DIAG_PATH = os.path.join(os.path.dirname(os.path.abspath(__file__)), "libnoa_dcs_diag.so")
+DIAG_SIGNATURES = {
+    "noa_dcs_probe_fma": (_INT, [_INT, _P, _INT, _INT, ctypes.POINTER(_D), _P]),
+    "noa_dcs_lean64_eval": (_INT, [_INT, _P, _P, _P, _I64, _P]),
+}
+
 _lib = None
+_diag = None
 
 
 def load(path=LIB_PATH):
@@ -103,6 +109,22 @@ def load(path=LIB_PATH):
         fn.restype = res
         fn.argtypes = args
     _lib = lib
+    return lib
+
+
+def load_diag(path=DIAG_PATH):
+    """Loads the test / bench instrument library once."""
+    global _diag
+    if _diag is not None:
+        return _diag
+    if not os.path.exists(path):
+        raise RuntimeError(f"{path} is not built; run `python -m noa_gb300.build`")
+    lib = ctypes.CDLL(path)
+    for name, (res, args) in DIAG_SIGNATURES.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    _diag = lib
     return lib
 
 

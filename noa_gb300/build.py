@@ -1,14 +1,19 @@
 """Build recipe for the native parts of noa_gb300 (no cmake).
 
     python -m noa_gb300.build            # CUDA library + CPU oracle
-    python -m noa_gb300.build --ref      # also the reference oracle (needs a noa checkout)
+    python -m noa_gb300.build --ref      # also the reference's own code (oracle/build_ref.sh)
 
 Products (all git-ignored, built in place):
     noa_gb300/libnoa_dcs.so      CUDA kernels + C ABI of include/noa_dcs.h, sm_103a only
     noa_gb300/libnoa_dcs_torch.so  LibTorch drop-in (include/noa_gb300/dcs_cuda.hh)
+    noa_gb300/libnoa_dcs_diag.so   test / bench instruments (csrc/diag/noa_dcs_diag.h), not the product
     noa_gb300/_muons_cuda*.so    Python module mirroring the reference notebook's extension
     oracle/liboracle_dcs.so      CPU restatement of the reference, the tests' oracle
-    oracle/_ref/libnoa_ref_dcs.so  the reference's own dcs.hh (only where a noa checkout exists)
+    oracle/_ref/libnoa_ref_dcs.so  the reference's own dcs.hh on the CPU
+    oracle/_ref/libnoa_ref_cuda.so the reference's own CUDA bremsstrahlung kernel
+    oracle/_ref/ref_dropin_caller  a reference-side program linked with libnoa_dcs_torch.so
+                                   (the three oracle/_ref products only where a noa checkout
+                                   or its staged headers exist; oracle/build_ref.sh)
 
 Each .cu file is compiled in its own nvcc process, in parallel, then linked.
 """
@@ -26,6 +31,8 @@ LIB = os.path.join(PKG, "libnoa_dcs.so")
 ORACLE_DIR = os.path.join(ROOT, "oracle")
 ORACLE_LIB = os.path.join(ORACLE_DIR, "liboracle_dcs.so")
 REF_LIB = os.path.join(ORACLE_DIR, "_ref", "libnoa_ref_dcs.so")
+REF_CUDA_LIB = os.path.join(ORACLE_DIR, "_ref", "libnoa_ref_cuda.so")
+REF_CALLER = os.path.join(ORACLE_DIR, "_ref", "ref_dropin_caller")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ARCH + ["-O3", "-std=c++17", "-lineinfo", "--expt-relaxed-constexpr",
@@ -66,6 +73,27 @@ def _stale(target, deps):
 def _headers():
     hs = [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".h", ".cuh"))]
     return hs + [os.path.join(ROOT, "include", "noa_dcs.h")]
+
+
+DIAG_DIR = os.path.join(CSRC, "diag")
+DIAG_LIB = os.path.join(PKG, "libnoa_dcs_diag.so")
+
+
+def build_diag():
+    """libnoa_dcs_diag.so: the test and bench instruments (FMA-chain peak
+    probe, element-wise evaluator of the library's elementary functions),
+    kept out of the product library libnoa_dcs.so."""
+    nvcc = _nvcc()
+    os.makedirs(BUILD, exist_ok=True)
+    srcs = sorted(os.path.join(DIAG_DIR, f) for f in os.listdir(DIAG_DIR) if f.endswith(".cu"))
+    deps = _headers() + [os.path.join(DIAG_DIR, "noa_dcs_diag.h")]
+    objs = [os.path.join(BUILD, "diag_" + os.path.basename(s)[:-3] + ".o") for s in srcs]
+    jobs = [(s, o) for s, o in zip(srcs, objs) if _stale(o, [s] + deps)]
+    with cf.ThreadPoolExecutor(max_workers=max(1, len(jobs))) as ex:
+        list(ex.map(lambda so: _run([nvcc] + NVCC_FLAGS + ["-c", so[0], "-o", so[1]]), jobs))
+    if jobs or _stale(DIAG_LIB, objs):
+        _run([nvcc] + ARCH + ["-shared", "-o", DIAG_LIB] + objs)
+    return DIAG_LIB
 
 
 def build_cuda(verbose=False):
@@ -147,27 +175,45 @@ def build_oracle():
     return ORACLE_LIB
 
 
-def build_ref(noa_checkout="/root/reference"):
-    """Compiles the reference's own dcs.hh behind oracle/ref_dcs_wrapper.cc.
-    Skipped (returns None) where no noa checkout is present."""
-    if not os.path.exists(os.path.join(noa_checkout, "src", "noa", "pms", "dcs.hh")):
-        return None
-    deps = [os.path.join(ORACLE_DIR, "ref_dcs_wrapper.cc")]
-    if _stale(REF_LIB, deps):
-        _run(["bash", os.path.join(ORACLE_DIR, "build_ref.sh"), noa_checkout])
-    return REF_LIB
+def build_ref(stage="all"):
+    """Builds the reference's own code with oracle/build_ref.sh (test and bench
+    infrastructure): stage "all" gives oracle/_ref/libnoa_ref_dcs.so (the
+    reference's CPU dcs::vmap / dcs::pvmap) and oracle/_ref/libnoa_ref_cuda.so
+    (its CUDA bremsstrahlung kernel); stage "caller" gives
+    oracle/_ref/ref_dropin_caller, linked with libnoa_dcs_torch.so.  The
+    script reads a noa checkout (NOA_CHECKOUT) or the copy of its headers
+    staged in oracle/_ref/src; with neither it does nothing and this returns
+    None.  A failure is recorded in oracle/_ref/build_<stage>.log and returns None:
+    the reference's code is a checker and a baseline, never a product
+    dependency, so it must not stop the product's build."""
+    log = os.path.join(ORACLE_DIR, "_ref", f"build_{stage}.log")
+    try:
+        text = _run(["bash", os.path.join(ORACLE_DIR, "build_ref.sh"), stage])
+    except RuntimeError as e:
+        text = str(e)
+        ok = False
+    else:
+        ok = True
+    if os.path.isdir(os.path.dirname(log)):
+        with open(log, "w") as f:
+            f.write(("ok\n" if ok else "FAILED\n") + text)
+    target = {"all": REF_LIB, "caller": REF_CALLER}[stage]
+    return target if ok and os.path.exists(target) else None
 
 
 def build_all(ref=True, torch_layer=True, verbose=False):
     with cf.ThreadPoolExecutor(max_workers=4) as ex:
         f_cuda = ex.submit(build_cuda, verbose)
+        f_diag = ex.submit(build_diag)
         f_oracle = ex.submit(build_oracle)
         f_ref = ex.submit(build_ref) if ref else None
         f_tobj = ex.submit(compile_torch_objects) if torch_layer else None
-        out = {"cuda": f_cuda.result(), "oracle": f_oracle.result()}
+        out = {"cuda": f_cuda.result(), "diag": f_diag.result(), "oracle": f_oracle.result()}
         out["ref"] = f_ref.result() if f_ref else None
         if torch_layer:
             out["torch"] = build_torch(f_tobj.result())
+    if ref and torch_layer:
+        out["ref_caller"] = build_ref("caller")
     return out
 
 

@@ -6,7 +6,11 @@
  * chains cannot be removed.  flops = 2 * CHAINS * iters * threads.
  * These kernels have no counterpart in the reference.
  */
-#include "dcs_launch.h"
+#include "noa_dcs_diag.h"
+
+#include "../../../include/noa_dcs.h"
+
+#include <cuda_runtime.h>
 
 namespace {
 

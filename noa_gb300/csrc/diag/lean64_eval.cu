@@ -1,13 +1,15 @@
 /*
- * Diagnostics entry point: evaluates one lean64 function (lean64.cuh), one
+ * Diagnostics entry point of libnoa_dcs_diag.so: evaluates one lean64 function (lean64.cuh), one
  * integer-pipe conversion (fpconv.cuh) or one float-float function
  * (dcs_fp32c.cuh) element-wise so that tests can bound its error against a
  * host libm, or check it bit for bit against the cast it replaces.  No
  * counterpart in the reference.
  */
-#include "dcs_fp32c.cuh"
-#include "dcs_launch.h"
-#include "lean64.cuh"
+#include "noa_dcs_diag.h"
+
+#include "../dcs_fp32c.cuh"
+#include "../dcs_launch.h"
+#include "../lean64.cuh"
 
 #include <initializer_list>
 

@@ -2,9 +2,11 @@
 
 Python access (ctypes) to oracle/liboracle_dcs.so, the scalar C++
 restatement in dcs_oracle.hpp of the reference's src/noa/pms/dcs.hh and
-physics.hh, and, where it was built (only on a host with a noa checkout), to
-oracle/_ref/libnoa_ref_dcs.so, the reference's own code.  Only tests/,
-__graft_entry__.smoke() and bench.py's CPU baseline may use this package; the
+physics.hh, and, where oracle/build_ref.sh built them (from a noa checkout or
+its staged headers), to the reference's own code: oracle/_ref/libnoa_ref_dcs.so
+(dcs.hh on the CPU), oracle/_ref/libnoa_ref_cuda.so (its CUDA bremsstrahlung
+kernel, dcs.cuh) and oracle/_ref/ref_dropin_caller.  Only tests/,
+__graft_entry__.smoke() and bench.py's baseline legs may use this package; the
 product (noa_gb300) never imports it.
 """
 import ctypes
@@ -14,7 +16,10 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 ORACLE_LIB = os.path.join(HERE, "liboracle_dcs.so")
-REF_LIB = os.path.join(HERE, "_ref", "libnoa_ref_dcs.so")
+REF_LIB = os.path.join(HERE, "_ref", "libnoa_ref_dcs.so")              # no FMA contraction: parity build
+REF_BENCH_LIB = os.path.join(HERE, "_ref", "libnoa_ref_dcs_bench.so")  # the reference benchmark's flags
+REF_CUDA_LIB = os.path.join(HERE, "_ref", "libnoa_ref_cuda.so")
+REF_CALLER = os.path.join(HERE, "_ref", "ref_dropin_caller")
 
 _P = ctypes.c_void_p
 _D = ctypes.c_double
@@ -23,7 +28,8 @@ _I32 = ctypes.c_int32
 _INT = ctypes.c_int
 
 _oracle = None
-_ref = None
+_ref = {}
+_ref_cuda = None
 
 
 def _ptr(a):
@@ -64,16 +70,19 @@ def _elastic_signatures(L, prefix):
         f.restype = _INT
 
 
-def ref_available():
-    return os.path.exists(REF_LIB)
+def ref_available(build="parity"):
+    return os.path.exists(REF_LIB if build == "parity" else REF_BENCH_LIB)
 
 
-def ref_lib():
-    global _ref
-    if _ref is None:
-        if not ref_available():
-            raise RuntimeError(f"{REF_LIB} is not built (needs a noa checkout)")
-        L = ctypes.CDLL(REF_LIB)
+def ref_lib(build="parity"):
+    """The compiled reference: build "parity" (-O3, no FMA contraction: bit
+    for bit the build that made the goldens) or "bench" (the reference
+    benchmark's flags, the compiler's default contraction)."""
+    if build not in _ref:
+        path = REF_LIB if build == "parity" else REF_BENCH_LIB
+        if not os.path.exists(path):
+            raise RuntimeError(f"{path} is not built (needs a noa checkout or its staged headers)")
+        L = ctypes.CDLL(path)
         L.ref_dcs_vmap.argtypes = [_INT, _INT, _P, _P, _P, _I64, _D, _D, _I32, _D]
         L.ref_dcs_vmap.restype = _INT
         L.ref_recoil_integral_vmap.argtypes = [_INT, _INT, _P, _P, _I64, _D, _D, _D, _I32, _D, _I32]
@@ -81,8 +90,37 @@ def ref_lib():
         _elastic_signatures(L, "ref")
         L.ref_soft_scattering.argtypes = [_P, _P, _I64, _D, _D, _I32, _D]
         L.ref_soft_scattering.restype = _INT
-        _ref = L
-    return _ref
+        _ref[build] = L
+    return _ref[build]
+
+
+def ref_cuda_available():
+    return os.path.exists(REF_CUDA_LIB)
+
+
+def ref_cuda_lib():
+    """The reference's CUDA bremsstrahlung kernel (dcs.cuh:30-41) behind
+    ref_cuda_vmap_bremsstrahlung(result, K, q, n, A, I, Z, mass): device
+    pointers of the current device, launched on the legacy default stream."""
+    global _ref_cuda
+    if _ref_cuda is None:
+        if not ref_cuda_available():
+            raise RuntimeError(f"{REF_CUDA_LIB} is not built (needs a noa checkout or its staged headers)")
+        L = ctypes.CDLL(REF_CUDA_LIB)
+        L.ref_cuda_vmap_bremsstrahlung.argtypes = [_P, _P, _P, _I64, _D, _D, _I32, _D]
+        L.ref_cuda_vmap_bremsstrahlung.restype = _INT
+        _ref_cuda = L
+    return _ref_cuda
+
+
+def ref_cuda_bremsstrahlung(result_ptr, K_ptr, q_ptr, n, element, mass):
+    """Enqueues the reference's own CUDA kernel on device buffers (raw
+    pointers); raises on a launch error."""
+    rc = ref_cuda_lib().ref_cuda_vmap_bremsstrahlung(_P(result_ptr), _P(K_ptr), _P(q_ptr), int(n),
+                                                     float(element.A), float(element.I), int(element.Z),
+                                                     float(mass))
+    if rc:
+        raise RuntimeError(f"reference CUDA kernel launch failed ({rc})")
 
 
 def dcs(process, K, q, element, mass, threads=0):
@@ -118,11 +156,11 @@ def opcount(process, K, q, element, mass):
     return dict(zip(("add", "mul", "div", "sqrt", "cmp", "trans"), c.tolist()))
 
 
-def ref_dcs(process, K, q, element, mass, parallel=False):
+def ref_dcs(process, K, q, element, mass, parallel=False, build="parity"):
     """The reference's own dcs::vmap (or dcs::pvmap) -- only where it was built."""
     K, q = _f64(K), _f64(q)
     out = np.empty_like(K)
-    rc = ref_lib().ref_dcs_vmap(int(process), int(bool(parallel)), _ptr(K), _ptr(q), _ptr(out), K.size,
+    rc = ref_lib(build).ref_dcs_vmap(int(process), int(bool(parallel)), _ptr(K), _ptr(q), _ptr(out), K.size,
                                 float(element.A), float(element.I), int(element.Z), float(mass))
     if rc:
         raise ValueError(f"ref_dcs_vmap failed ({rc})")

@@ -1,8 +1,9 @@
 """Generates tests/golden/dcs_golden.npz from the REFERENCE's own code.
 
-Run where a grinisrit/noa checkout exists (default /root/reference):
+Run where a grinisrit/noa checkout exists, naming it by argument or by the
+NOA_CHECKOUT environment variable:
 
-    python tests/golden/make_golden.py [NOA_CHECKOUT]
+    python tests/golden/make_golden.py NOA_CHECKOUT
 
 It compiles the unmodified src/noa/pms/dcs.hh behind oracle/ref_dcs_wrapper.cc
 (oracle/build_ref.sh), evaluates it through the reference's dcs::vmap and
@@ -84,8 +85,11 @@ def edge_cases():
 
 
 def main():
-    noa = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
-    subprocess.run(["bash", os.path.join(ROOT, "oracle", "build_ref.sh"), noa], check=True)
+    noa = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("NOA_CHECKOUT")
+    if not noa or not os.path.exists(os.path.join(noa, "src", "noa", "pms", "dcs.hh")):
+        sys.exit("make_golden.py: name a grinisrit/noa checkout (argument or NOA_CHECKOUT)")
+    subprocess.run(["bash", os.path.join(ROOT, "oracle", "build_ref.sh"), "all"], check=True,
+                   env={**os.environ, "NOA_CHECKOUT": noa})
     out = {}
     Ks, qs = kinetic_recoil(N_SEEDED)
     import torch

@@ -1,5 +1,6 @@
 """CPU checks of bench.py's contract: the flop numerator re-derived from the
-oracle's operation count, and the reference arm's JSON line."""
+oracle's operation count, the reference arm's JSON line, and the summary
+digest printed last on the line."""
 import json
 import subprocess
 import sys
@@ -28,6 +29,34 @@ def test_reference_arm_prints_one_json_line(built):
     assert len(lines) == 1
     d = json.loads(lines[0])
     assert d["impl"] == "reference" and d["unit"] == "evals/s" and d["value"] > 0
-    assert d["cpu_baseline"]["kind"] == "port" and d["cpu_baseline"]["cores"] >= 1
+    # the reference's own dcs::pvmap where oracle/build_ref.sh compiled it, else the port
+    assert d["cpu_baseline"]["kind"] == ("reference" if oracle.ref_available() else "port")
+    assert d["cpu_baseline"]["cores"] >= 1
     assert d["e2e"]["h2d_bytes_per_step"] == 0 and d["e2e"]["value"] == d["value"]
     assert d["metric"] == bench.METRIC and d["higher_is_better"] is True
+
+
+def test_summary_is_last_and_compact():
+    """summarise() on a line shaped like the GPU arm's, with every optional
+    section present: the digest stays a few kB and is the line's last key."""
+    per = {p: {"evals_per_s": 1e9, "ms_per_launch": 1.0, "speedup_vs_fp64": 10.0, "max_rel": 9e-7,
+               "median_rel": 5e-8, "mean_rel": 6e-8, "zero_pattern_equal": True} for p in bench.PROCESSES}
+    per["all_processes"] = {"evals_per_s": 2e10, "speedup_vs_fp64": 12.0}
+    line = {"value": 1.6e9, "config": bench.config_dict(100_000_000, 1), "e2e": {"value": 1.5e9},
+            "roofline": {"frac": 0.7}, "variants": {"fp32c": per},
+            "parity_vs_oracle": {"sample": "x", **{p: {"mean_rel": 1e-15, "max_rel": 1e-11, "cond_ratio": 0.01,
+                                                       "zero_pattern_equal": True} for p in bench.PROCESSES}},
+            "reference_cuda_bremsstrahlung": {"available": True, "ms_per_launch": 30.0, "ours_ms_per_launch": 13.6,
+                                              "speedup_of_ours": 2.2, "vs_ours": {"mean_rel": 1e-16}},
+            "batched": {"fp64": {"all_processes": {"evals_per_s": 1.6e9}},
+                        "fp32c": {"all_processes": {"evals_per_s": 1.5e10}}},
+            "surrogate": {"error_bound": 1e-3, **{p: {"speedup_vs_fp64": 11.0, "speedup_vs_fp32c": 1.3,
+                                                      "max_rel": 5e-4, "frac_above_1e-3": 0.0,
+                                                      "network_share_of_open": 0.3,
+                                                      "training": {"train_seconds": 30.0}}
+                                                  for p in ("pair_production", "photonuclear")}},
+            "cpu_baseline": {"value": 1e8, "kind": "reference", "cores": 16}}
+    line["summary"] = bench.summarise(line)
+    text = json.dumps(line)
+    assert list(json.loads(text))[-1] == "summary"
+    assert len(json.dumps(line["summary"])) < 2500

@@ -29,6 +29,21 @@ def test_library_exports_every_declared_symbol(built):
     assert not missing
 
 
+DIAG_HEADER = os.path.join(os.path.dirname(HEADER), os.pardir, "noa_gb300", "csrc", "diag", "noa_dcs_diag.h")
+
+
+def test_instruments_live_outside_the_product_library(built):
+    """The FMA probe and the function evaluator are declared in the
+    instrument header and exported by libnoa_dcs_diag.so only."""
+    diag = declared_functions(DIAG_HEADER)
+    assert diag == sorted(_lib.DIAG_SIGNATURES)
+    assert not set(diag) & set(declared_functions())
+    product = ctypes.CDLL(_lib.LIB_PATH)
+    assert not any(hasattr(product, f) for f in diag)
+    inst = ctypes.CDLL(_lib.DIAG_PATH)
+    assert all(hasattr(inst, f) for f in diag)
+
+
 def test_abi_version_and_status_strings(built):
     lib = _lib.load()
     assert lib.noa_dcs_abi_version() == 1

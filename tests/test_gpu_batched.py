@@ -50,9 +50,10 @@ def test_ten_elements_uneven(cuda_device, process, precision):
     o = 0
     for z, c, exp in zip(BATCH_Z, SMALL_COUNTS, segment_oracle(process, BATCH_Z, SMALL_COUNTS, K, q)):
         seg = got[o:o + c]
+        Ks, qs = K[o:o + c], q[o:o + c]
         o += c
         if precision == "fp64":
-            assert_fp64_parity(seg, exp, f"Z={z}")
+            assert_fp64_parity(seg, exp, f"Z={z}", inputs=(process, Ks, qs, ELEMENTS[z], MUON_MASS))
         else:
             s = rel_stats(seg, exp)
             assert s["zero_agree"] and s["max"] <= 1e-6, (z, s)

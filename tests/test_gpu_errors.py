@@ -14,7 +14,7 @@ pytestmark = pytest.mark.gpu
 
 
 def test_diagnostics_reject_host_buffers(cuda_device):
-    lib = _lib.load()
+    lib = _lib.load_diag()
     host = np.zeros(64)
     dev = torch.zeros(64, dtype=torch.float64, device="cuda")
     assert lib.noa_dcs_lean64_eval(0, host.ctypes.data, None, dev.data_ptr(), 64, None) == _lib.ERROR_NOT_DEVICE_MEMORY

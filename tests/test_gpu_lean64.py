@@ -10,7 +10,7 @@ pytestmark = pytest.mark.gpu
 
 
 def run(fn, x, y=None):
-    lib = _lib.load()
+    lib = _lib.load_diag()
     tx = torch.from_numpy(np.ascontiguousarray(x)).cuda()
     ty = torch.from_numpy(np.ascontiguousarray(y)).cuda() if y is not None else tx
     out = torch.empty_like(tx)

@@ -33,7 +33,7 @@ def test_seeded_parity_fp64(cuda_device, process, z):
     K, q = kinetic_recoil(1 << 16, offset=1 << 20)
     el = ELEMENTS[z]
     s = assert_fp64_parity(gpu_dcs(process, K, q, el), oracle.dcs(process, K, q, el, MUON_MASS),
-                           f"{PROCESSES[process]} Z={z}")
+                           f"{PROCESSES[process]} Z={z}", inputs=(process, K, q, el, MUON_MASS))
     print(PROCESSES[process], z, s)
 
 
@@ -41,7 +41,8 @@ def test_seeded_parity_fp64(cuda_device, process, z):
 def test_tau_mass_parity(cuda_device, process):
     K, q = kinetic_recoil(1 << 14, offset=3 << 20)
     assert_fp64_parity(gpu_dcs(process, K, q, STANDARD_ROCK, TAU_MASS),
-                       oracle.dcs(process, K, q, STANDARD_ROCK, TAU_MASS), PROCESSES[process])
+                       oracle.dcs(process, K, q, STANDARD_ROCK, TAU_MASS), PROCESSES[process],
+                       inputs=(process, K, q, STANDARD_ROCK, TAU_MASS))
 
 
 @pytest.mark.parametrize("process", range(4), ids=PROCESSES)
@@ -52,8 +53,10 @@ def test_golden_vectors(cuda_device, golden, process, subset):
         key = f"{subset}_{ename}_{PROCESSES[process]}"
         if key not in golden:
             continue
-        got = gpu_dcs(process, golden[f"{subset}_K"], golden[f"{subset}_q"], AtomicElement(A, I, Z))
-        assert_fp64_parity(got, golden[key], key)
+        el = AtomicElement(A, I, Z)
+        K, q = golden[f"{subset}_K"], golden[f"{subset}_q"]
+        got = gpu_dcs(process, K, q, el)
+        assert_fp64_parity(got, golden[key], key, inputs=(process, K, q, el, MUON_MASS))
 
 
 @pytest.mark.parametrize("process", range(4), ids=PROCESSES)
@@ -62,7 +65,8 @@ def test_ragged_sizes(cuda_device, process, n):
     K, q = kinetic_recoil(n, offset=999)
     got = gpu_dcs(process, K, q)
     assert not np.any(got == -7.0)
-    assert_fp64_parity(got, oracle.dcs(process, K, q, STANDARD_ROCK, MUON_MASS), f"n={n}")
+    assert_fp64_parity(got, oracle.dcs(process, K, q, STANDARD_ROCK, MUON_MASS), f"n={n}",
+                       inputs=(process, K, q, STANDARD_ROCK, MUON_MASS))
 
 
 @pytest.mark.parametrize("process", range(4), ids=PROCESSES)
@@ -92,7 +96,8 @@ def test_result_may_alias_an_input(cuda_device, process):
     tq = torch.from_numpy(q).cuda()
     dcs.vmap(process, tk, tk, tq)   # result written over K, as the reference allows
     torch.cuda.synchronize()
-    assert_fp64_parity(tk.cpu().numpy(), oracle.dcs(process, K, q, STANDARD_ROCK, MUON_MASS), "alias")
+    assert_fp64_parity(tk.cpu().numpy(), oracle.dcs(process, K, q, STANDARD_ROCK, MUON_MASS), "alias",
+                       inputs=(process, K, q, STANDARD_ROCK, MUON_MASS))
 
 
 def test_error_paths_with_device_memory(cuda_device):
@@ -178,7 +183,8 @@ def test_large_size_properties(cuda_device, process):
     assert torch.equal(a[perm], c)
     idx = np.random.default_rng(11).choice(n, 200_000, replace=False)
     got = a.cpu().numpy()[idx]
-    assert_fp64_parity(got, oracle.dcs(process, K[idx], q[idx], STANDARD_ROCK, MUON_MASS), "1e7 sample")
+    assert_fp64_parity(got, oracle.dcs(process, K[idx], q[idx], STANDARD_ROCK, MUON_MASS), "1e7 sample",
+                       inputs=(process, K[idx], q[idx], STANDARD_ROCK, MUON_MASS))
     assert np.all(np.isfinite(a.cpu().numpy()))
 
 

@@ -26,7 +26,7 @@ def test_notebook_style_call(muons_cuda, process):
     q = 0.0505 * K
     got = getattr(muons_cuda, PROCESSES[process])(K.cuda(), q.cuda()).cpu().numpy()
     exp = oracle.dcs(process, K.numpy(), q.numpy(), STANDARD_ROCK, MUON_MASS)
-    assert_fp64_parity(got, exp, PROCESSES[process])
+    assert_fp64_parity(got, exp, PROCESSES[process], inputs=(process, K.numpy(), q.numpy(), STANDARD_ROCK, MUON_MASS))
 
 
 def test_notebook_cpu_gpu_agreement_like_the_reference(muons_cuda):

@@ -72,9 +72,28 @@ def test_oracle_serial_equals_openmp(built, process):
 @pytest.mark.parametrize("process", range(4), ids=PROCESSES)
 @pytest.mark.parametrize("z", [1, 8, 11, 26, 82])
 def test_oracle_matches_compiled_reference(built, process, z):
+    """Bit for bit against the reference compiled without FMA contraction
+    (the build that made the goldens, on any host)."""
     K, q = kinetic_recoil(50000, offset=123456)
     el = ELEMENTS[z]
     assert same_bits(oracle.dcs(process, K, q, el, MUON_MASS), oracle.ref_dcs(process, K, q, el, MUON_MASS))
+
+
+@pytest.mark.skipif(not oracle.ref_available("bench"), reason="reference not compiled on this host")
+@pytest.mark.parametrize("process", range(4), ids=PROCESSES)
+@pytest.mark.parametrize("z", [1, 11, 82])
+def test_benchmark_build_of_the_reference_meets_the_fp64_bar(built, process, z):
+    """The timed CPU baseline is the reference built with its benchmark's
+    flags; where the compiler fuses a*b + c (aarch64) its last bits move, so
+    it is held to the FP64 bar (mean, per-point conditioning, zero pattern)
+    against the oracle, and it runs dcs::pvmap and dcs::vmap identically."""
+    from tests.parity import assert_fp64_parity
+    K, q = kinetic_recoil(50000, offset=654321)
+    el = ELEMENTS[z]
+    got = oracle.ref_dcs(process, K, q, el, MUON_MASS, parallel=True, build="bench")
+    assert same_bits(got, oracle.ref_dcs(process, K, q, el, MUON_MASS, parallel=False, build="bench"))
+    assert_fp64_parity(got, oracle.dcs(process, K, q, el, MUON_MASS), f"{PROCESSES[process]} Z={z}",
+                       inputs=(process, K, q, el, MUON_MASS))
 
 
 @pytest.mark.parametrize("process", range(4), ids=PROCESSES)
