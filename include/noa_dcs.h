@@ -192,17 +192,21 @@ const char *noa_dcs_batch_last_error(void);
  * work of one batch plan execution -- process, precision (FP32C at tolerance
  * 1e-6), segments (at most 16: larger counts of segments are rejected with
  * NOA_DCS_ERROR_INVALID_VALUE) -- without a plan and without allocating
- * anything.  For callers that may not allocate device memory during the
- * call: code that runs it inside its own stream capture, where cudaMalloc is
- * forbidden, or a host application that owns all device memory through its
- * own arena.  The engine's one piece of scratch, a tile counter, lives in a
- * 256-byte static device array that every device loading the library keeps
- * until exit; each call zeroes it on `stream` before the launch.  All calls
- * share that array: calls whose work overlaps on the GPU (different streams,
- * or different host threads) race and must be serialised by the caller.  The
- * first call on each device looks up the array's device address (with that
- * device current) and must come before any stream capture.  Tile shape is
- * fixed (256 threads x 4 pairs, 2 CTAs per SM).  Buffers as for the plan. */
+ * anything.  For callers that cannot let a library allocate device memory:
+ * an application that hands all of the GPU's memory to its own arena or pool
+ * at start-up, so a cudaMalloc from this library would fail or escape its
+ * accounting, or a transport code whose stepping loop may not pay for an
+ * allocation's device synchronisation.  The engine's one piece of scratch, a
+ * tile counter, lives in a 256-byte static device array that every device
+ * loading the library keeps until exit; each call zeroes it on `stream`
+ * before the launch.  All calls share that array: calls whose work overlaps
+ * on the GPU (different streams, or different host threads) race and must be
+ * serialised by the caller.  Set-up on the first call on each device: the
+ * array's device address is looked up with that device current, and for
+ * FP32C pair production (54 KB of shared memory) the kernel's shared-memory
+ * limit is raised; make that first call before any stream capture.  Tile
+ * shape is fixed (256 threads x 4 pairs, 2 CTAs per SM).  Buffers as for the
+ * plan. */
 int noa_dcs_cuda_vmap_batched_noalloc(int process, int precision, int n_segments, const noa_dcs_element *elements,
                                       const int64_t *counts, double mass, double *result, const double *K,
                                       const double *q, void *stream);

@@ -48,6 +48,19 @@ int bfail(int st, const char *msg, cudaError_t e = cudaSuccess) {
     return st;
 }
 
+// Non-negative segment counts whose running sum stays within INT64_MAX / 8,
+// so that the tile ranges and the byte sizes of the overlap checks cannot
+// overflow.
+bool counts_fit(const int64_t *counts, int n_segments) {
+    int64_t total = 0;
+    for (int s = 0; s < n_segments; s++) {
+        if (counts[s] > INT64_MAX / 8 - total)
+            return false;
+        total += counts[s];
+    }
+    return true;
+}
+
 size_t smem_bytes(const noa_dcs_batch_plan *p, int threads, int items) {
     const bool third = noa_dcs::batch_third_queue(p->process, p->precision);
     return threads == 128 ? noa_dcs::BatchSmem<128>::bytes(items, third)
@@ -151,6 +164,8 @@ int noa_dcs_batch_plan_create(noa_dcs_batch_plan **out_plan, int process, int pr
         if (counts[s] < 0)
             return bfail(NOA_DCS_ERROR_INVALID_VALUE, "negative segment count");
     }
+    if (!counts_fit(counts, n_segments))
+        return bfail(NOA_DCS_ERROR_INVALID_VALUE, "segment counts add up past INT64_MAX / 8");
     noa_dcs_batch_plan *p = new (std::nothrow) noa_dcs_batch_plan();
     if (!p)
         return bfail(NOA_DCS_ERROR_INVALID_VALUE, "out of host memory");
@@ -358,11 +373,10 @@ const char *noa_dcs_batch_last_error(void) { return g_err; }
 
 // ---------------------------------------------------------------- allocation-free batched entry point
 //
-// Some callers may not allocate device memory during a call: a transport
-// code that evaluates cross-sections from inside its own CUDA-graph capture
-// (cudaMalloc is not allowed while a stream is being captured), or a host
-// application that has reserved the GPU's memory for its own arena and owns
-// every allocation.  For them the batched engine also runs with its only
+// Some callers cannot let a library allocate device memory: a host
+// application that gives all of the GPU's memory to its own arena at
+// start-up and owns every allocation, or a transport loop that may not pay
+// for an allocation's device synchronisation.  For them the batched engine also runs with its only
 // scratch -- the 64-bit tile counter -- in the static device array below
 // instead of in a plan.  Every device that loads this library holds these
 // 256 bytes until the process exits.
@@ -419,6 +433,8 @@ extern "C" int noa_dcs_cuda_vmap_batched_noalloc(int process, int precision, int
         if (counts[s] < 0)
             return bfail(NOA_DCS_ERROR_INVALID_VALUE, "negative segment count");
     }
+    if (!counts_fit(counts, n_segments))
+        return bfail(NOA_DCS_ERROR_INVALID_VALUE, "segment counts add up past INT64_MAX / 8");
     cudaError_t e = cudaGetDevice(&p.device);
     if (e == cudaSuccess)
         e = cudaDeviceGetAttribute(&p.sms, cudaDevAttrMultiProcessorCount, p.device);
@@ -435,7 +451,9 @@ extern "C" int noa_dcs_cuda_vmap_batched_noalloc(int process, int precision, int
         noa_dcs_fill_consts(&p.params.consts[s], elements[s].A, elements[s].I, elements[s].Z, mass);
     }
     // Fixed tile shape (the plan default): 256 threads x 4 pairs, 2 CTAs per
-    // SM; its 43 KB of shared memory needs no opt-in attribute.
+    // SM.  Its queues take 43 KB of shared memory, 54 KB for FP32C pair
+    // production (a third queue); above 48 KB the launch raises the kernel's
+    // limit once per device, on its first call there.
     p.threads = 256;
     p.items = 4;
     p.ctas_per_sm = 2;

@@ -29,6 +29,8 @@
 #include "dcs_fp64.cuh"
 #include "dcs_launch.h"
 
+#include <atomic>
+
 namespace noa_dcs {
 
 struct BatchParams {
@@ -327,6 +329,34 @@ __global__ void __launch_bounds__(THREADS) dcs_batched_kernel(const __grid_const
         __syncthreads();
         qn += tile_open;
     }
+}
+
+// Raises a kernel's dynamic shared-memory limit to the device's opt-in
+// maximum once per device (`done` is the kernel's own flag table), so that
+// only the first launch on a device above 48 KB sets a function attribute and
+// later launches, including launches inside a caller's stream capture, set
+// none.
+constexpr int kSmemOptinDevices = 64;
+template <typename Kernel>
+inline cudaError_t smem_optin_once(Kernel k, size_t smem, std::atomic<bool> (&done)[kSmemOptinDevices]) {
+    if (smem <= 48 * 1024)
+        return cudaSuccess;
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess)
+        return e;
+    if (dev >= 0 && dev < kSmemOptinDevices && done[dev].load(std::memory_order_acquire))
+        return cudaSuccess;
+    int optin = 0;
+    e = cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    if (e != cudaSuccess)
+        return e;
+    if (smem > (size_t)optin)
+        return cudaErrorInvalidValue;
+    e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
+    if (e == cudaSuccess && dev >= 0 && dev < kSmemOptinDevices)
+        done[dev].store(true, std::memory_order_release);
+    return e;
 }
 
 } // namespace noa_dcs

@@ -7,14 +7,16 @@
 
 namespace noa_dcs {
 
+// One opt-in flag table per kernel instantiation (see smem_optin_once).
+template <int PROC, int THREADS>
+static std::atomic<bool> g_optin[kSmemOptinDevices];
+
 template <int PROC, int THREADS>
 static cudaError_t launch_one(const void *params, int grid, size_t smem, cudaStream_t s) {
     auto k = dcs_batched_kernel<PROC, NOA_DCS_FP64, THREADS>;
-    if (smem > 48 * 1024) {
-        const cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        if (e != cudaSuccess)
-            return e;
-    }
+    const cudaError_t e = smem_optin_once(k, smem, g_optin<PROC, THREADS>);
+    if (e != cudaSuccess)
+        return e;
     k<<<grid, THREADS, smem, s>>>(*static_cast<const BatchParams *>(params));
     return cudaGetLastError();
 }
@@ -22,8 +24,10 @@ static cudaError_t launch_one(const void *params, int grid, size_t smem, cudaStr
 template <int PROC, int THREADS>
 static int occupancy_one(size_t smem) {
     auto k = dcs_batched_kernel<PROC, NOA_DCS_FP64, THREADS>;
-    if (smem > 48 * 1024)
-        cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (smem_optin_once(k, smem, g_optin<PROC, THREADS>) != cudaSuccess) {
+        cudaGetLastError();
+        return 0;
+    }
     int n = 0;
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k, THREADS, smem) != cudaSuccess) {
         cudaGetLastError();

@@ -107,3 +107,19 @@ def test_python_surface_type_errors():
                                 torch.zeros(3, dtype=torch.float64))
     with pytest.raises(RuntimeError):   # CPU tensors are not CUDA tensors
         dcs.vmap_bremsstrahlung(*(torch.zeros(3, dtype=torch.float64) for _ in range(3)))
+
+
+def test_segment_counts_that_overflow_are_rejected_without_a_gpu(built):
+    """Counts whose running sum passes INT64_MAX / 8 would wrap the tile
+    ranges; the plan and the allocation-free entry point refuse them before
+    any CUDA call."""
+    lib = _lib.load()
+    els = (_lib.Element * 2)(_lib.element_struct(STANDARD_ROCK), _lib.element_struct(STANDARD_ROCK))
+    big = (1 << 63) - 1
+    for counts in ([big // 8, 1], [big, big]):
+        cnt = (ctypes.c_int64 * 2)(*counts)
+        plan = ctypes.c_void_p()
+        assert lib.noa_dcs_batch_plan_create(ctypes.byref(plan), 0, 0, 2, els, cnt, MUON_MASS) == 1
+        assert b"INT64_MAX" in lib.noa_dcs_batch_last_error()
+        assert lib.noa_dcs_cuda_vmap_batched_noalloc(0, 0, 2, els, cnt, MUON_MASS, None, None, None, None) == 1
+        assert b"INT64_MAX" in lib.noa_dcs_batch_last_error()

@@ -109,3 +109,35 @@ def test_float_float_exp_log(host_lib):
     big = np.abs(ref) > 0.1
     assert (err[big] / np.abs(ref[big]).astype(np.float64)).max() <= 5e-13
     assert err[~big].max() <= 3e-14
+
+
+def test_pair_production_estimate_near_the_recalibration_pair(host_lib):
+    """A standard-rock pair near K = 0.74 GeV, q = 0.55 GeV (just below the
+    upper bound q = K + m (1 - 0.75 sqrt(e) Z^1/3) ~ K - 0.185 GeV, the
+    electron screening term clamped, the muon screening log ~0.28) was once
+    accepted by the float form at an error of 1.06e-6: the muon screening
+    log's absolute float error reaches ~4 u there.  On 1.2e6 pairs packed
+    around it (K and q/K within 5%, and 2e5 of them within 1e-3), plus 1e6
+    pairs at q/K ~ 0.68 where most are accepted, the estimate bounds every
+    open pair's error, and no accepted pair exceeds the 1e-6 tolerance, in
+    the float and the float-float form.  (Errors there reach ~1.3e-6, so the
+    pairs nearest the point must be, and are, rejected.)"""
+    rng = np.random.default_rng(74)
+    nu0 = 0.55 / 0.74
+    K = np.concatenate([0.74 * (1 + rng.uniform(-0.05, 0.05, 1_000_000)),
+                        0.74 * (1 + rng.uniform(-1e-3, 1e-3, 200_000)),
+                        0.74 * (1 + rng.uniform(-0.05, 0.05, 1_000_000))])
+    nu = np.concatenate([nu0 * (1 + rng.uniform(-0.05, 0.05, 1_000_000)),
+                         nu0 * (1 + rng.uniform(-1e-3, 1e-3, 200_000)),
+                         0.5 / 0.74 * (1 + rng.uniform(-0.05, 0.05, 1_000_000))])
+    q = nu * K
+    ref = oracle.dcs(1, K, q, STANDARD_ROCK, MUON_MASS)
+    nz = ref != 0
+    assert nz.sum() > 1_500_000
+    for mode in (0, 1):
+        out, est = evaluate(host_lib, 1, K, q, STANDARD_ROCK, mode)
+        err = np.abs(out[nz] - ref[nz]) / ref[nz]
+        assert np.all(err < est[nz]), (mode, float((err / est[nz]).max()))
+        acc = est[nz] <= 1e-6
+        assert acc.sum() > 500_000
+        assert err[acc].max() < 1e-6, (mode, float(err[acc].max()))

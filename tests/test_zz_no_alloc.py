@@ -1,11 +1,10 @@
 """Allocation-free batched entry point, noa_dcs_cuda_vmap_batched_noalloc.
 
-Some callers of this library may not let it allocate device memory while
-they call it: a particle-transport code that evaluates cross-sections from
-inside its own CUDA-graph capture (cudaMalloc is forbidden while a stream is
-captured), or an application that has reserved the GPU's memory for its own
-arena.  This entry point serves them by keeping its only scratch, the
-engine's tile counter, in a static device array.  Its results must equal
+Some callers of this library cannot let it allocate device memory: an
+application that has given all of the GPU's memory to its own arena at
+start-up, or a particle-transport loop that may not pay for an allocation's
+device synchronisation.  This entry point serves them by keeping its only
+scratch, the engine's tile counter, in a static device array.  Its results must equal
 those of the plan-based batched entry point, on two calls in a row: the
 second call runs on the scratch the first one left behind.
 """
