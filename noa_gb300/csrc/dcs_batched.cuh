@@ -331,11 +331,11 @@ __global__ void __launch_bounds__(THREADS) dcs_batched_kernel(const __grid_const
     }
 }
 
-// Raises a kernel's dynamic shared-memory limit to the device's opt-in
-// maximum once per device (`done` is the kernel's own flag table), so that
-// only the first launch on a device above 48 KB sets a function attribute and
-// later launches, including launches inside a caller's stream capture, set
-// none.
+// Raises a kernel's dynamic shared-memory limit once per device to the most
+// it can take (the device's opt-in maximum less the kernel's static shared
+// memory; `done` is the kernel's own flag table), so that only the first
+// launch on a device above 48 KB sets a function attribute and later
+// launches, including launches inside a caller's stream capture, set none.
 constexpr int kSmemOptinDevices = 64;
 template <typename Kernel>
 inline cudaError_t smem_optin_once(Kernel k, size_t smem, std::atomic<bool> (&done)[kSmemOptinDevices]) {
@@ -351,9 +351,14 @@ inline cudaError_t smem_optin_once(Kernel k, size_t smem, std::atomic<bool> (&do
     e = cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
     if (e != cudaSuccess)
         return e;
-    if (smem > (size_t)optin)
+    cudaFuncAttributes fa;
+    e = cudaFuncGetAttributes(&fa, k);
+    if (e != cudaSuccess)
+        return e;
+    const int max_dynamic = optin - (int)fa.sharedSizeBytes;
+    if (max_dynamic <= 0 || smem > (size_t)max_dynamic)
         return cudaErrorInvalidValue;
-    e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
+    e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, max_dynamic);
     if (e == cudaSuccess && dev >= 0 && dev < kSmemOptinDevices)
         done[dev].store(true, std::memory_order_release);
     return e;

@@ -39,6 +39,7 @@
 #include "dcs_fp64.cuh"
 #include "dcs_launch.h"
 #include "mlp.cuh"
+#include "tcgen05.cuh"
 
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
@@ -57,7 +58,6 @@ constexpr int TMEM_COLS = 512;            // per slot: accumulator 128 + A hi 64
 constexpr int MAT = H * H * 2;            // bytes of one 128 x 128 BF16 operand
 constexpr int SMEM_NET = 4 * MAT + 1024;  // W2 hi/lo, W3 hi/lo, alignment slack
 constexpr int MAX_EL = 16;
-constexpr long long SPIN_LIMIT = 1LL << 26;
 
 struct InferParams {
     const double *K;
@@ -337,88 +337,17 @@ __global__ void __launch_bounds__(256) fallback_kernel(const __grid_constant__ I
     }
 }
 
-// ---------------------------------------------------------------- tcgen05 helpers
-__device__ __forceinline__ uint32_t smem_u32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
-
-// Offset of element (r, k) in a 128 x 128 BF16 operand in the canonical
-// K-major no-swizzle layout: 8 x 8 core matrices of 128 contiguous bytes,
-// K-adjacent core matrices 128 B apart (LBO), 8-row groups 2048 B apart (SBO).
-__device__ __forceinline__ uint32_t canon_off(int r, int k) {
-    return (uint32_t)((r >> 3) * 2048 + (k >> 3) * 128 + (r & 7) * 16 + (k & 7) * 2);
-}
-
-// Shared-memory matrix descriptor (tcgen05 format): start address, LBO and
-// SBO in units of 16 B, descriptor version 1 (bits 46-47), no swizzle.
-__device__ __forceinline__ uint64_t make_desc(uint32_t saddr) {
-    const uint64_t lbo = 128 >> 4, sbo = 2048 >> 4;
-    return (uint64_t)((saddr & 0x3FFFF) >> 4) | (lbo << 16) | (sbo << 32) | (1ULL << 46);
-}
-
-// Instruction descriptor, kind::f16: D FP32, A and B BF16, both K-major,
-// N = 128, M = 128.
-constexpr uint32_t IDESC = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(128 >> 3) << 17) |
-                           ((uint32_t)(128 >> 4) << 24);
-
-__device__ __forceinline__ void mma_commit(uint32_t mbar) {
-    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(mbar)
-                 : "memory");
-}
-
-// Bounded wait for the mbarrier phase `parity`; false on expiry.
-__device__ __forceinline__ bool mbar_wait(uint32_t mbar, uint32_t parity) {
-    for (long long it = 0; it < SPIN_LIMIT; it++) {
-        uint32_t done;
-        asm volatile("{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
-                     "selp.u32 %0, 1, 0, p;\n\t}"
-                     : "=r"(done)
-                     : "r"(mbar), "r"(parity)
-                     : "memory");
-        if (done)
-            return true;
-    }
-    return false;
-}
-
-__device__ __forceinline__ void tmem_ld32(uint32_t taddr, float (&v)[32]) {
-    uint32_t r[32];
-    asm volatile("tcgen05.ld.sync.aligned.32x32b.x32.b32 "
-                 "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
-                 "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
-                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
-                   "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]),
-                   "=r"(r[14]), "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]),
-                   "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]),
-                   "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
-                 : "r"(taddr));
-    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-#pragma unroll
-    for (int i = 0; i < 32; i++)
-        v[i] = __uint_as_float(r[i]);
-}
-
-__device__ __forceinline__ void fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
-__device__ __forceinline__ void fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
-__device__ __forceinline__ void fence_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
-
-// Stores 16 consecutive 32-bit TMEM columns of this warp's 32 lanes.
-__device__ __forceinline__ void tmem_st16(uint32_t taddr, const uint32_t (&r)[16]) {
-    asm volatile("tcgen05.st.sync.aligned.32x32b.x16.b32 [%0], "
-                 "{%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16};"
-                 :
-                 : "r"(taddr), "r"(r[0]), "r"(r[1]), "r"(r[2]), "r"(r[3]), "r"(r[4]), "r"(r[5]), "r"(r[6]),
-                   "r"(r[7]), "r"(r[8]), "r"(r[9]), "r"(r[10]), "r"(r[11]), "r"(r[12]), "r"(r[13]), "r"(r[14]),
-                   "r"(r[15])
-                 : "memory");
-}
-
-// MMA with the A operand in TMEM (M = 128 lanes, two BF16 per 32-bit column)
-// and B from shared memory.
-__device__ __forceinline__ void mma_f16_ts(uint32_t d_tmem, uint32_t a_tmem, uint64_t b, uint32_t accumulate) {
-    asm volatile("{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
-                 "tcgen05.mma.cta_group::1.kind::f16 [%0], [%1], %2, %3, p;\n\t}"
-                 :
-                 : "r"(d_tmem), "r"(a_tmem), "l"(b), "r"(IDESC), "r"(accumulate));
-}
+// ---------------------------------------------------------------- tcgen05 helpers (tcgen05.cuh)
+using noa_tc::canon_off;
+using noa_tc::fence_after;
+using noa_tc::fence_async_smem;
+using noa_tc::fence_before;
+using noa_tc::make_desc;
+using noa_tc::mbar_wait;
+using noa_tc::mma_commit;
+using noa_tc::smem_u32;
+using noa_tc::tmem_ld32;
+using noa_tc::tmem_st16;
 
 // Packs 32 activations (consecutive hidden units, even unit in the low half)
 // as BF16 hi / lo pairs: 16 + 16 32-bit TMEM columns.
@@ -443,9 +372,9 @@ __device__ __forceinline__ void issue_layer_ts(uint32_t acc, uint32_t a_hi, uint
     for (int ks = 0; ks < 8; ks++) {
         const uint32_t o = ks * 256;  // B: two core matrices along K per step
         const uint32_t c = ks * 8;    // A: 16 BF16 = 8 TMEM columns per step
-        mma_f16_ts(acc, a_hi + c, make_desc(w_hi + o), ks > 0);
-        mma_f16_ts(acc, a_lo + c, make_desc(w_hi + o), 1);
-        mma_f16_ts(acc, a_hi + c, make_desc(w_lo + o), 1);
+        noa_tc::mma_ts(acc, a_hi + c, make_desc(w_hi + o), ks > 0);
+        noa_tc::mma_ts(acc, a_lo + c, make_desc(w_hi + o), 1);
+        noa_tc::mma_ts(acc, a_hi + c, make_desc(w_lo + o), 1);
     }
     mma_commit(mbar);
 }

@@ -3,9 +3,10 @@
  * kernels and the C ABI of the model object (include/noa_dcs.h,
  * noa_dcs_mlp_*).  No counterpart in the reference.
  *
- * Training runs on the tensor cores in BF16 with FP32 accumulation
- * (mma.sync m16n8k16): the 128 x 128 products of the two hidden layers, their
- * input gradients and their weight gradients.  The first layer (4 inputs) and
+ * Training runs on the 5th-generation tensor cores (tcgen05.mma, operands in
+ * shared memory, FP32 accumulator in TMEM; tcgen05.cuh) in BF16 with FP32
+ * accumulation: the 128 x 128 products of the two hidden layers, their input
+ * gradients and their weight gradients.  The first layer (4 inputs) and
  * the output layer (1 output) are FP32 on the CUDA cores.  In the forward
  * products both the hidden activations and the weights enter as a BF16 hi +
  * lo pair (x = hi + lo, 16 significant bits), as three products
@@ -18,12 +19,14 @@
 #include "dcs_fp64.cuh"
 #include "dcs_launch.h"
 #include "mlp.cuh"
+#include "tcgen05.cuh"
 
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
 #include <initializer_list>
 
+#include <atomic>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -33,144 +36,198 @@ using namespace noa_mlp;
 
 namespace {
 
-constexpr int LD = H + 8;  // padded bf16 row of a 128-wide smem tile (ldmatrix without bank conflicts)
 constexpr int G_THREADS = 256;
-constexpr size_t G_SMEM = 4u * H * LD * sizeof(__nv_bfloat16);
+constexpr int G_TMEM_COLS = 128;  // the 128 x 128 FP32 accumulator
+using noa_tc::MAT_BYTES;
 
 enum { G_FWD = 0, G_DX = 1, G_DW = 2 };
 
-__device__ __forceinline__ void ldsm_x4(unsigned &r0, unsigned &r1, unsigned &r2, unsigned &r3, const void *p) {
-    const unsigned a = (unsigned)__cvta_generic_to_shared(p);
-    asm volatile("ldmatrix.sync.aligned.m8n8.x4.shared.b16 {%0,%1,%2,%3}, [%4];"
-                 : "=r"(r0), "=r"(r1), "=r"(r2), "=r"(r3)
-                 : "r"(a));
-}
-__device__ __forceinline__ void ldsm_x4_t(unsigned &r0, unsigned &r1, unsigned &r2, unsigned &r3, const void *p) {
-    const unsigned a = (unsigned)__cvta_generic_to_shared(p);
-    asm volatile("ldmatrix.sync.aligned.m8n8.x4.trans.shared.b16 {%0,%1,%2,%3}, [%4];"
-                 : "=r"(r0), "=r"(r1), "=r"(r2), "=r"(r3)
-                 : "r"(a));
-}
-__device__ __forceinline__ void mma_bf16(float (&d)[4], const unsigned (&a)[4], unsigned b0, unsigned b1) {
-    asm volatile("mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
-                 "{%0,%1,%2,%3};"
-                 : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
-                 : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
+// Dynamic shared memory of a mode: FWD stages A hi / lo and W hi / lo, the
+// gradient modes one A and one B operand; 1 KB of alignment slack.
+template <int MODE>
+constexpr size_t gemm_smem() {
+    return (MODE == G_FWD ? 4u : 2u) * MAT_BYTES + 1024u;
 }
 
 struct GemmArgs {
-    const float *A;        // FWD: layer input H [M][128]; DX, DW: dZ [M][128]
-    const float *B;        // DW: H_prev [M][128]
+    const float *A;         // FWD: layer input H [M][128]; DX, DW: dZ [M][128]
+    const float *B;         // DW: H_prev [M][128]
     const __nv_bfloat16 *W; // FWD, DX: weights [128 out][128 in] (hi); FWD also reads lo at W + 2*128*128
-    const float *bias;     // FWD
-    const float *zprev;    // DX: pre-activation of the previous layer [M][128]
-    float *outZ;           // FWD: Z; DX: dZ_prev
-    float *outH;           // FWD: H = silu(Z)
-    float *dW;             // DW: [128 out][128 in], accumulated
-    float *db;             // DW: [128], accumulated
+    const float *bias;      // FWD
+    const float *zprev;     // DX: pre-activation of the previous layer [M][128]
+    float *outZ;            // FWD: Z; DX: dZ_prev
+    float *outH;            // FWD: H = silu(Z)
+    float *dW;              // DW: [128 out][128 in], accumulated
+    float *db;              // DW: [128], accumulated
+    unsigned int *status;   // set to NOA_DCS_ERROR_TIMEOUT if an mbarrier wait expires
     int M;
 };
 
-// One CTA, 8 warps, a 128 x 128 output tile; warp w owns rows 16w..16w+15.
-//   FWD: Z = A W^T + b (A split hi/lo), H = silu(Z)
-//   DX : dZ_prev = (dZ W) * silu'(z_prev)
-//   DW : dW += dZ^T H_prev over this CTA's 128 samples, db += sum dZ
+// 8 FP32 values -> 8 BF16 (hi), and the rounding residues as 8 BF16 (lo).
+__device__ __forceinline__ void split8(const float (&v)[8], uint4 &hi, uint4 &lo) {
+    uint32_t h[4], l[4];
+#pragma unroll
+    for (int i = 0; i < 4; i++) {
+        const __nv_bfloat162 ph = __floats2bfloat162_rn(v[2 * i], v[2 * i + 1]);
+        const float2 back = __bfloat1622float2(ph);
+        const __nv_bfloat162 pl = __floats2bfloat162_rn(v[2 * i] - back.x, v[2 * i + 1] - back.y);
+        h[i] = *reinterpret_cast<const uint32_t *>(&ph);
+        l[i] = *reinterpret_cast<const uint32_t *>(&pl);
+    }
+    hi = make_uint4(h[0], h[1], h[2], h[3]);
+    lo = make_uint4(l[0], l[1], l[2], l[3]);
+}
+
+// One CTA per 128-row tile, on the 5th-generation tensor cores:
+//   FWD: Z = A W^T + b with A and W as BF16 hi + lo pairs (three products
+//        A_hi W_hi + A_lo W_hi + A_hi W_lo), H = silu(Z)
+//   DX : dZ_prev = (dZ W) * silu'(z_prev)          (B operand = W^T)
+//   DW : dW += dZ^T H_prev over this tile's samples  (M = out, N = in, K = samples)
+// The operands are staged as BF16 in shared memory in the canonical K-major
+// layout (tcgen05.cuh): item e covers row r = e % 128 and the 8 K-consecutive
+// elements k0 .. k0 + 7, k0 = 8 (e / 128), one 16-byte store per item (a warp
+// stores 32 rows of one K-block: conflict-free).  Where the product needs a
+// transposed operand (DX's W^T, DW's dZ^T and H_prev^T) the 8 elements come
+// from 8 source rows at column r, which across a warp are coalesced reads.
+// One thread issues the MMAs into a 128-column TMEM accumulator and commits
+// to an mbarrier; every thread waits (bounded), then warp w reads TMEM lanes
+// 32 (w % 4) .. + 31 (rows) and columns 64 (w / 4) .. + 63 for the epilogue.
 template <int MODE>
-__global__ void __launch_bounds__(G_THREADS) mlp_gemm_kernel(const GemmArgs g) {
-    extern __shared__ __align__(16) unsigned char sm[];
-    __nv_bfloat16 *sA = reinterpret_cast<__nv_bfloat16 *>(sm);
-    __nv_bfloat16 *sAl = sA + H * LD;
-    __nv_bfloat16 *sB = sAl + H * LD;
-    __nv_bfloat16 *sBl = sB + H * LD;
+__global__ void __launch_bounds__(G_THREADS, 1) mlp_gemm_kernel(const GemmArgs g) {
+    using namespace noa_tc;
+    extern __shared__ unsigned char smem_raw[];
+    unsigned char *sm = smem_raw + ((1024 - (smem_u32(smem_raw) & 1023)) & 1023);
+    unsigned char *sA = sm, *sB = sm + MAT_BYTES;
+    unsigned char *sAl = sm + 2 * MAT_BYTES, *sBl = sm + 3 * MAT_BYTES;  // FWD only
+    __shared__ uint32_t tmem_slot;
+    __shared__ __align__(8) unsigned long long mbar;
     const int row0 = blockIdx.x * H;
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
 
-    // stage operands (FP32 -> BF16; FWD keeps the rounding residue as lo)
-    for (int e = tid; e < H * H; e += G_THREADS) {
-        const int r = e / H, c = e % H;
-        const bool in = row0 + r < g.M;
-        const float a = in ? g.A[(size_t)(row0 + r) * H + c] : 0.f;
-        const __nv_bfloat16 ah = __float2bfloat16_rn(a);
-        sA[r * LD + c] = ah;
-        if (MODE == G_FWD)
-            sAl[r * LD + c] = __float2bfloat16_rn(a - __bfloat162float(ah));
-        if (MODE == G_DW)
-            sB[r * LD + c] = __float2bfloat16_rn(in ? g.B[(size_t)(row0 + r) * H + c] : 0.f);
-        else
-            sB[r * LD + c] = g.W[r * H + c];
-        if (MODE == G_FWD)
-            sBl[r * LD + c] = g.W[2 * H * H + r * H + c];
+    if (warp == 0)
+        tmem_alloc(smem_u32(&tmem_slot), G_TMEM_COLS);
+    if (tid == 0) {
+        mbar_init(smem_u32(&mbar), 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
-    __syncthreads();
 
-    float acc[16][4];
-#pragma unroll
-    for (int i = 0; i < 16; i++)
-        acc[i][0] = acc[i][1] = acc[i][2] = acc[i][3] = 0.f;
-    const int mi = lane >> 3, mr = lane & 7;  // which 8x8 matrix this lane addresses, and its row
-#pragma unroll 1
-    for (int ks = 0; ks < H / 16; ks++) {
-        const int k0 = ks * 16;
-        unsigned a[4], al[4];
+    // stage the operands
+    for (int e = tid; e < H * H / 8; e += G_THREADS) {
+        const int r = e % H, k0 = (e / H) * 8;
+        const uint32_t o = canon_off(r, k0);
+        float v[8];
         if (MODE == G_DW) {
-            // A_op[m][k] = dZ[k][m]: transposed loads of the stored [k][m] tile
-            const int kr = k0 + (mi >> 1) * 8 + mr, mc = warp * 16 + (mi & 1) * 8;
-            ldsm_x4_t(a[0], a[1], a[2], a[3], sA + kr * LD + mc);
-        } else {
-            const int r = warp * 16 + (mi & 1) * 8 + mr, c = k0 + (mi >> 1) * 8;
-            ldsm_x4(a[0], a[1], a[2], a[3], sA + r * LD + c);
-            if (MODE == G_FWD)
-                ldsm_x4(al[0], al[1], al[2], al[3], sAl + r * LD + c);
-        }
+            // A(r = out, k = sample) = dZ[k][r]; B(r = in, k = sample) = H_prev[k][r]
+            float w[8];
 #pragma unroll
-        for (int nb = 0; nb < 16; nb += 2) {
-            unsigned b0, b1, b2, b3, l0 = 0, l1 = 0, l2 = 0, l3 = 0;
-            if (MODE == G_FWD) {
-                // B_op[k][n] = W[n][k]: rows n of W, k contiguous
-                const int n = nb * 8 + (mi >> 1) * 8 + mr, c = k0 + (mi & 1) * 8;
-                ldsm_x4(b0, b1, b2, b3, sB + n * LD + c);
-                ldsm_x4(l0, l1, l2, l3, sBl + n * LD + c);
-            } else {
-                // B_op[k][n] stored [k][n] (DX: W[out][in]; DW: H_prev[sample][in]): transposed loads
-                const int k = k0 + (mi & 1) * 8 + mr, c = nb * 8 + (mi >> 1) * 8;
-                ldsm_x4_t(b0, b1, b2, b3, sB + k * LD + c);
+            for (int j = 0; j < 8; j++) {
+                const bool in = row0 + k0 + j < g.M;
+                v[j] = in ? g.A[(size_t)(row0 + k0 + j) * H + r] : 0.f;
+                w[j] = in ? g.B[(size_t)(row0 + k0 + j) * H + r] : 0.f;
             }
-            mma_bf16(acc[nb], a, b0, b1);
-            mma_bf16(acc[nb + 1], a, b2, b3);
+            uint4 hi, lo;
+            split8(v, hi, lo);
+            *reinterpret_cast<uint4 *>(sA + o) = hi;
+            split8(w, hi, lo);
+            *reinterpret_cast<uint4 *>(sB + o) = hi;
+        } else {
+            // A(r = sample, k) = A[r][k]
+            if (row0 + r < g.M) {
+                const float4 *src = reinterpret_cast<const float4 *>(g.A + (size_t)(row0 + r) * H + k0);
+                const float4 x = src[0], y = src[1];
+                v[0] = x.x, v[1] = x.y, v[2] = x.z, v[3] = x.w, v[4] = y.x, v[5] = y.y, v[6] = y.z, v[7] = y.w;
+            } else {
+#pragma unroll
+                for (int j = 0; j < 8; j++)
+                    v[j] = 0.f;
+            }
+            uint4 hi, lo;
+            split8(v, hi, lo);
+            *reinterpret_cast<uint4 *>(sA + o) = hi;
             if (MODE == G_FWD) {
-                mma_bf16(acc[nb], al, b0, b1);
-                mma_bf16(acc[nb + 1], al, b2, b3);
-                mma_bf16(acc[nb], a, l0, l1);
-                mma_bf16(acc[nb + 1], a, l2, l3);
+                *reinterpret_cast<uint4 *>(sAl + o) = lo;
+                // B(r = out, k = in) = W[r][k], hi and lo
+                *reinterpret_cast<uint4 *>(sB + o) = *reinterpret_cast<const uint4 *>(g.W + r * H + k0);
+                *reinterpret_cast<uint4 *>(sBl + o) = *reinterpret_cast<const uint4 *>(g.W + 2 * H * H + r * H + k0);
+            } else {
+                // DX: B(r = in, k = out) = W[k][r]
+                uint32_t b[4];
+#pragma unroll
+                for (int j = 0; j < 4; j++) {
+                    const __nv_bfloat162 t = __halves2bfloat162(g.W[(k0 + 2 * j) * H + r], g.W[(k0 + 2 * j + 1) * H + r]);
+                    b[j] = *reinterpret_cast<const uint32_t *>(&t);
+                }
+                *reinterpret_cast<uint4 *>(sB + o) = make_uint4(b[0], b[1], b[2], b[3]);
             }
         }
     }
+    fence_async_smem();
+    fence_before();
+    __syncthreads();
+    fence_after();
+    const uint32_t acc = tmem_slot;
+    const uint32_t mb = smem_u32(&mbar);
 
-    // epilogue: acc[nb] = rows (r, r+8), cols (c, c+1)
-    const int r = warp * 16 + (lane >> 2), cq = (lane & 3) * 2;
+    if (tid == 0) {
+        const uint32_t a0 = smem_u32(sA), b0 = smem_u32(sB), al0 = smem_u32(sAl), bl0 = smem_u32(sBl);
 #pragma unroll
-    for (int nb = 0; nb < 16; nb++) {
+        for (int ks = 0; ks < 8; ks++) {
+            const uint32_t o = ks * 256;  // 16 K-elements = two core matrices
+            const uint64_t a = make_desc(a0 + o), b = make_desc(b0 + o);
+            mma_ss(acc, a, b, ks > 0);
+            if (MODE == G_FWD) {
+                mma_ss(acc, make_desc(al0 + o), b, 1);
+                mma_ss(acc, a, make_desc(bl0 + o), 1);
+            }
+        }
+        mma_commit(mb);
+    }
+    const bool ok = mbar_wait(mb, 0);
+    fence_after();
+
+    if (ok) {
+        const int row = (warp & 3) * 32 + lane;
+        const uint32_t lane_base = (uint32_t)((warp & 3) * 32) << 16;
+#pragma unroll 1
+        for (int half = 0; half < 2; half++) {
+            const int c0 = (warp >> 2) * 64 + half * 32;
+            float v[32];
+            tmem_ld32(acc + lane_base + (uint32_t)c0, v);
+            if (MODE == G_DW) {
+                // row = out index, column = in index
 #pragma unroll
-        for (int h = 0; h < 2; h++) {
-            const int rr = r + h * 8;
+                for (int j = 0; j < 32; j++)
+                    atomicAdd(&g.dW[row * H + c0 + j], v[j]);
+            } else if (row0 + row < g.M) {
+                const size_t o = (size_t)(row0 + row) * H + c0;
+                if (MODE == G_FWD) {
 #pragma unroll
-            for (int j = 0; j < 2; j++) {
-                const int cc = nb * 8 + cq + j;
-                const float v = acc[nb][h * 2 + j];
-                if (MODE == G_DW) {
-                    atomicAdd(&g.dW[rr * H + cc], v);
-                } else if (row0 + rr < g.M) {
-                    const size_t o = (size_t)(row0 + rr) * H + cc;
-                    if (MODE == G_FWD) {
-                        const float z = v + g.bias[cc];
-                        g.outZ[o] = z;
-                        g.outH[o] = silu(z);
-                    } else {
-                        g.outZ[o] = v * dsilu(g.zprev[o]);
+                    for (int j = 0; j < 32; j += 4) {
+                        float4 z, h;
+                        z.x = v[j] + g.bias[c0 + j];
+                        z.y = v[j + 1] + g.bias[c0 + j + 1];
+                        z.z = v[j + 2] + g.bias[c0 + j + 2];
+                        z.w = v[j + 3] + g.bias[c0 + j + 3];
+                        h.x = silu(z.x), h.y = silu(z.y), h.z = silu(z.z), h.w = silu(z.w);
+                        *reinterpret_cast<float4 *>(g.outZ + o + j) = z;
+                        *reinterpret_cast<float4 *>(g.outH + o + j) = h;
+                    }
+                } else {
+#pragma unroll
+                    for (int j = 0; j < 32; j += 4) {
+                        const float4 zp = *reinterpret_cast<const float4 *>(g.zprev + o + j);
+                        float4 d;
+                        d.x = v[j] * dsilu(zp.x), d.y = v[j + 1] * dsilu(zp.y);
+                        d.z = v[j + 2] * dsilu(zp.z), d.w = v[j + 3] * dsilu(zp.w);
+                        *reinterpret_cast<float4 *>(g.outZ + o + j) = d;
                     }
                 }
             }
         }
+    } else {
+        if (lane == 0)
+            atomicMax(g.status, (unsigned int)NOA_DCS_ERROR_TIMEOUT);
+        mbar_wait(mb, 0);  // one more bounded wait before the TMEM it writes is freed
     }
     if (MODE == G_DW && tid < H) {
         float s = 0.f;
@@ -178,6 +235,11 @@ __global__ void __launch_bounds__(G_THREADS) mlp_gemm_kernel(const GemmArgs g) {
             s += g.A[(size_t)(row0 + k) * H + tid];
         atomicAdd(&g.db[tid], s);
     }
+    fence_before();
+    __syncthreads();
+    fence_after();
+    if (warp == 0)
+        tmem_dealloc(acc, G_TMEM_COLS);
 }
 
 // Layer 1 (FP32): Z1 = X W1^T + b1, H1 = silu(Z1).
@@ -345,6 +407,7 @@ struct noa_dcs_mlp {
     float *Z1 = nullptr, *H1 = nullptr, *Z2 = nullptr, *H2 = nullptr, *Z3 = nullptr, *H3 = nullptr;
     float *D3 = nullptr, *D2 = nullptr, *D1 = nullptr;
     float *loss = nullptr;
+    unsigned int *status = nullptr;  // device word, see take_status
     int64_t step = 0;
     float norm[2 * IN + 2] = {};
 };
@@ -361,19 +424,33 @@ int mfail(int st, const char *msg, cudaError_t e = cudaSuccess) {
     return st;
 }
 
+// Raises the three GEMM kernels' dynamic shared-memory limits once per device
+// (called when a model is created).
 cudaError_t set_gemm_smem() {
-    static bool done = false;
-    if (done)
+    static std::atomic<bool> done[64];
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess)
+        return e;
+    if (dev >= 0 && dev < 64 && done[dev].load())
         return cudaSuccess;
-    cudaError_t e = cudaFuncSetAttribute(mlp_gemm_kernel<G_FWD>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)G_SMEM);
+    e = cudaFuncSetAttribute(mlp_gemm_kernel<G_FWD>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)gemm_smem<G_FWD>());
     if (e == cudaSuccess)
-        e = cudaFuncSetAttribute(mlp_gemm_kernel<G_DX>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)G_SMEM);
+        e = cudaFuncSetAttribute(mlp_gemm_kernel<G_DX>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)gemm_smem<G_DX>());
     if (e == cudaSuccess)
-        e = cudaFuncSetAttribute(mlp_gemm_kernel<G_DW>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)G_SMEM);
-    done = e == cudaSuccess;
+        e = cudaFuncSetAttribute(mlp_gemm_kernel<G_DW>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)gemm_smem<G_DW>());
+    if (e == cudaSuccess && dev >= 0 && dev < 64)
+        done[dev].store(true);
     return e;
 }
+
+// Status word of the tensor-core kernels: NOA_DCS_ERROR_TIMEOUT after an
+// expired mbarrier wait.  Read (and cleared) after the work of a call;
+// synchronises the stream.
+int take_status(noa_dcs_mlp *m, cudaStream_t s);
 
 // Forward over M <= batch rows already in m->Xb; prediction to pred if given.
 cudaError_t forward(noa_dcs_mlp *m, int M, float *pred, cudaStream_t s) {
@@ -381,18 +458,19 @@ cudaError_t forward(noa_dcs_mlp *m, int M, float *pred, cudaStream_t s) {
     mlp_fwd1_kernel<<<(M * H + 255) / 256, 256, 0, s>>>(m->Xb, m->P, m->Z1, m->H1, M);
     GemmArgs g{};
     g.M = M;
+    g.status = m->status;
     g.A = m->H1;
     g.W = m->Wb;
     g.bias = m->P + OFF_B2;
     g.outZ = m->Z2;
     g.outH = m->H2;
-    mlp_gemm_kernel<G_FWD><<<tiles, G_THREADS, G_SMEM, s>>>(g);
+    mlp_gemm_kernel<G_FWD><<<tiles, G_THREADS, gemm_smem<G_FWD>(), s>>>(g);
     g.A = m->H2;
     g.W = m->Wb + H * H;
     g.bias = m->P + OFF_B3;
     g.outZ = m->Z3;
     g.outH = m->H3;
-    mlp_gemm_kernel<G_FWD><<<tiles, G_THREADS, G_SMEM, s>>>(g);
+    mlp_gemm_kernel<G_FWD><<<tiles, G_THREADS, gemm_smem<G_FWD>(), s>>>(g);
     if (pred)
         mlp_out_kernel<<<tiles, 128, 0, s>>>(m->H3, m->Z3, nullptr, m->P, nullptr, nullptr, nullptr, M, 0.f, pred);
     return cudaGetLastError();
@@ -410,26 +488,27 @@ cudaError_t backward(noa_dcs_mlp *m, int M, cudaStream_t s) {
                                          nullptr);
     GemmArgs g{};
     g.M = M;
+    g.status = m->status;
     // layer 3: dW3 = dZ3^T H2, dZ2 = (dZ3 W3) silu'(Z2)
     g.A = m->D3;
     g.B = m->H2;
     g.dW = m->G + OFF_W3;
     g.db = m->G + OFF_B3;
-    mlp_gemm_kernel<G_DW><<<tiles, G_THREADS, G_SMEM, s>>>(g);
+    mlp_gemm_kernel<G_DW><<<tiles, G_THREADS, gemm_smem<G_DW>(), s>>>(g);
     g.W = m->Wb + H * H;
     g.zprev = m->Z2;
     g.outZ = m->D2;
-    mlp_gemm_kernel<G_DX><<<tiles, G_THREADS, G_SMEM, s>>>(g);
+    mlp_gemm_kernel<G_DX><<<tiles, G_THREADS, gemm_smem<G_DX>(), s>>>(g);
     // layer 2: dW2 = dZ2^T H1, dZ1 = (dZ2 W2) silu'(Z1)
     g.A = m->D2;
     g.B = m->H1;
     g.dW = m->G + OFF_W2;
     g.db = m->G + OFF_B2;
-    mlp_gemm_kernel<G_DW><<<tiles, G_THREADS, G_SMEM, s>>>(g);
+    mlp_gemm_kernel<G_DW><<<tiles, G_THREADS, gemm_smem<G_DW>(), s>>>(g);
     g.W = m->Wb;
     g.zprev = m->Z1;
     g.outZ = m->D1;
-    mlp_gemm_kernel<G_DX><<<tiles, G_THREADS, G_SMEM, s>>>(g);
+    mlp_gemm_kernel<G_DX><<<tiles, G_THREADS, gemm_smem<G_DX>(), s>>>(g);
     mlp_bwd1_kernel<<<tiles, 128, 0, s>>>(m->D1, m->Xb, m->G, M);
     return cudaGetLastError();
 }
@@ -453,6 +532,20 @@ bool device_ok(std::initializer_list<const void *> ptrs) {
             return false;
     }
     return true;
+}
+
+int take_status(noa_dcs_mlp *m, cudaStream_t s) {
+    unsigned int st = 0;
+    cudaError_t e = cudaMemcpyAsync(&st, m->status, sizeof st, cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess)
+        e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess)
+        return mfail(NOA_DCS_ERROR_CUDA, "status read", e);
+    if (st) {
+        cudaMemsetAsync(m->status, 0, sizeof st, s);
+        return mfail((int)st, "a tensor-core wait expired (mbarrier); the results of this call are invalid");
+    }
+    return NOA_DCS_SUCCESS;
 }
 
 } // namespace
@@ -487,7 +580,7 @@ int noa_dcs_mlp_create(noa_dcs_mlp **out, int process, int batch) {
     if (e == cudaSuccess)
         e = cudaMalloc((void **)&m->Wb, sizeof(__nv_bfloat16) * 4 * H * H);
     if (e == cudaSuccess)
-        e = cudaMalloc((void **)&m->Xb, sizeof(float) * (size_t)batch * (IN + 1) + sizeof(float));
+        e = cudaMalloc((void **)&m->Xb, sizeof(float) * (size_t)batch * (IN + 1) + 2 * sizeof(float));
     if (e != cudaSuccess) {
         for (float **a : acts)
             cudaFree(*a);
@@ -502,7 +595,9 @@ int noa_dcs_mlp_create(noa_dcs_mlp **out, int process, int batch) {
     m->V = m->Mm + NPARAM;
     m->Tb = m->Xb + (size_t)batch * IN;
     m->loss = m->Tb + batch;
+    m->status = reinterpret_cast<unsigned int *>(m->loss + 1);
     cudaMemset(m->P, 0, sizeof(float) * NPARAM * 4);
+    cudaMemset(m->status, 0, sizeof(unsigned int));
     cudaMemset(m->Wb, 0, sizeof(__nv_bfloat16) * 4 * H * H);
     *out = m;
     return NOA_DCS_SUCCESS;
@@ -624,7 +719,7 @@ int noa_dcs_mlp_train(noa_dcs_mlp *m, const float *X, const float *T, int64_t n,
     }
     if (e != cudaSuccess)
         return mfail(NOA_DCS_ERROR_CUDA, "training step", e);
-    return NOA_DCS_SUCCESS;
+    return take_status(m, s);
 }
 
 int noa_dcs_mlp_predict(noa_dcs_mlp *m, const float *X, float *out, int64_t n, void *stream) {
@@ -641,7 +736,7 @@ int noa_dcs_mlp_predict(noa_dcs_mlp *m, const float *X, float *out, int64_t n, v
         if (e != cudaSuccess)
             return mfail(NOA_DCS_ERROR_CUDA, "forward", e);
     }
-    return NOA_DCS_SUCCESS;
+    return n > 0 ? take_status(m, s) : NOA_DCS_SUCCESS;
 }
 
 int noa_dcs_mlp_gradient(noa_dcs_mlp *m, const float *X, const float *T, int n, float *grad, float *loss,
@@ -662,7 +757,7 @@ int noa_dcs_mlp_gradient(noa_dcs_mlp *m, const float *X, const float *T, int n, 
         e = cudaMemcpyAsync(loss, m->loss, sizeof(float), cudaMemcpyDeviceToDevice, s);
     if (e != cudaSuccess)
         return mfail(NOA_DCS_ERROR_CUDA, "gradient", e);
-    return NOA_DCS_SUCCESS;
+    return take_status(m, s);
 }
 
 int noa_dcs_mlp_destroy(noa_dcs_mlp *m) {

@@ -216,32 +216,68 @@ class Surrogate:
         c = (elem.long() * GRID[0] + ik.clamp(0, GRID[0] - 1)) * GRID[1] + inu.clamp(0, GRID[1] - 1)
         return torch.where(inside, c, torch.full_like(c, -1))
 
-    def build_trust(self, Xraw, R, valid, elem, bound=1e-3, safety=0.35, min_count=16, open_zero=None):
-        """Trust grid from a held-out set: a cell is trusted when all its
-        held-out samples have |predicted - true| log DCS below safety * bound
-        (|d log DCS| is the relative DCS error to first order), it holds at
-        least min_count of them, and none of its held-out pairs is open by the
-        kinematic bounds with DCS = 0 (the network cannot return 0).  The
-        held-out maximum of a cell only estimates the cell's true maximum:
-        with safety 0.5 and 8 samples, 2 of 1e8 bench queries reached
-        1.06e-3, hence 0.35 and 16."""
+    def lattice(self, points=7):
+        """A points x points lattice of (K, q) spanning every trust-grid cell
+        of every element, its edges and corners included: returns (K, q,
+        element index, cell index) as numpy arrays."""
+        gk, gn = GRID
+        dk = (LOGK_RANGE[1] - LOGK_RANGE[0]) / gk
+        dn = (LOGNU_RANGE[1] - LOGNU_RANGE[0]) / gn
+        t = np.linspace(0.0, 1.0, points)
+        ik, inu, a, b = np.meshgrid(np.arange(gk), np.arange(gn), t, t, indexing="ij")
+        lk = (LOGK_RANGE[0] + (ik + a) * dk).ravel()
+        ln = (LOGNU_RANGE[0] + (inu + b) * dn).ravel()
+        cell2 = (ik * gn + inu).ravel()
+        n_el = len(self.elements_z)
+        K = np.tile(np.exp(lk), n_el)
+        q = np.tile(np.exp(ln), n_el) * (K + self.mass)   # nu = q / (K + m), as the features
+        elem = np.repeat(np.arange(n_el, dtype=np.uint8), lk.size)
+        cell = elem.astype(np.int64) * (gk * gn) + np.tile(cell2, n_el)
+        return K, q, elem, cell
+
+    def build_trust(self, Xraw, R, valid, elem, bound=1e-3, safety=0.35, open_zero=None, lattice_points=7):
+        """Trust grid.  A cell is trusted when (1) every point of a
+        lattice_points x lattice_points lattice spanning it, edges and corners
+        included, is open with a non-zero DCS and has |predicted - true|
+        log DCS (the relative DCS error to first order) at most safety *
+        bound, and (2) so do all of its samples in the random held-out set
+        (Xraw, R, valid, elem: features, residuals and validity from
+        prepare()), none of which may be open with DCS = 0 (open_zero).  The
+        lattice takes every cell that touches a kinematic edge (DCS -> 0, where
+        log DCS is steep) out, and bounds the error of a smooth network between
+        its points; the random samples cover the cell's interior at other
+        positions.  The true maximum inside a cell is still only estimated,
+        hence the safety factor."""
+        ncell = len(self.elements_z) * GRID[0] * GRID[1]
+        lim = safety * bound
+        # (1) the lattice
+        Kl, ql, el, cl = self.lattice(lattice_points)
+        Xl, Rl, vl, _ = self.prepare(Kl, ql, el)
+        cl = torch.as_tensor(cl, device="cuda")
+        ok = torch.zeros(Kl.size, dtype=torch.bool, device="cuda")
+        if bool(vl.any()):
+            Xn = self.normalise(Xl[vl])
+            errl = (self.residual(self.predict(Xn)) - Rl[vl]).abs()
+            ok[vl] = errl <= lim
+        bad = torch.zeros(ncell, dtype=torch.int64, device="cuda")
+        bad.scatter_add_(0, cl, (~ok).long())
+        trust = bad == 0
+        lattice_trusted = int(trust.sum())
+        # (2) the random held-out set
         Xv, Rv, ev = Xraw[valid], R[valid], elem[valid]
         X, _ = self.normalise(Xv, Rv)
         err = (self.residual(self.predict(X)) - Rv).abs()
         cell = self.cells(Xv, ev)
-        ncell = len(self.elements_z) * GRID[0] * GRID[1]
         keep = cell >= 0
         worst = torch.zeros(ncell, dtype=torch.float32, device="cuda")
-        count = torch.zeros(ncell, dtype=torch.int64, device="cuda")
         worst.scatter_reduce_(0, cell[keep], err[keep], reduce="amax")
-        count.scatter_add_(0, cell[keep], torch.ones_like(cell[keep]))
-        trust = (worst <= safety * bound) & (count >= min_count)
+        trust &= worst <= lim
         if open_zero is not None and bool(open_zero.any()):
             zc = self.cells(Xraw[open_zero], elem[open_zero])
             zc = zc[zc >= 0]
             trust[zc] = False
         self.trust = trust.to(torch.uint8).cpu().numpy().reshape(len(self.elements_z), *GRID)
-        return {"cells_trusted": int(trust.sum()), "cells_with_data": int((count > 0).sum()),
+        return {"cells_trusted": int(trust.sum()), "cells_lattice_ok": lattice_trusted,
                 "heldout_err_max": float(err.max()), "heldout_err_median": float(err.median()),
                 "heldout_frac_trusted": float(trust[cell[keep]].float().mean())}
 
