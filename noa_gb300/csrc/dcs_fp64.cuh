@@ -112,29 +112,35 @@ static __device__ __noinline__ bool pprod_live_tail(double K, double q, double m
     return !((am >= 1.) || (am <= 0.));
 }
 
+// The whole open / closed decision in the reference's IEEE arithmetic
+// (dcs.hh:151-156 and the argmin check), out of line: reached only where float
+// cannot decide, so that the inlined fast path carries no FP64 comparison
+// (the compiler would otherwise evaluate the short exact tests
+// unconditionally, as predicated FP64 instructions, for every pair).
+static __device__ __noinline__ bool pprod_live_exact(double K, double q, double mass, double shift,
+                                                     float inv_mass_h, float inv_mass_l) {
+    if (q <= 4. * ME)
+        return false;
+    if (q >= K + shift)
+        return false;
+    return pprod_live_tail(K, q, mass, inv_mass_h, inv_mass_l, 1.f);
+}
+
 __device__ __forceinline__ bool pprod_live(double K, double q, const noa_dcs_consts &c) {
     const float Kf = fpconv::f32(K), qf = fpconv::f32(q);
-    if (!(Kf > 1e-20f && Kf < 1e30f && qf > 1e-20f && qf < 1e30f)) {
-        // outside the float-safe range (and NaN): the reference's IEEE checks
-        if (q <= 4. * ME)
-            return false;
-        if (q >= K + c.pp_kmax_shift)
-            return false;
-        return pprod_live_tail(K, q, c.mass, c.inv_mass_h, c.inv_mass_l, 1.f);
-    }
+    if (!(Kf > 1e-20f && Kf < 1e30f && qf > 1e-20f && qf < 1e30f))  // outside the float-safe range (and NaN)
+        return pprod_live_exact(K, q, c.mass, c.pp_kmax_shift, c.inv_mass_h, c.inv_mass_l);
     // q <= 4 me and q >= K + m (1 - 0.75 sqrt(e) Z^1/3) (dcs.hh:151-156) in
     // float, with the IEEE comparison within a relative margin of 1e-5
     constexpr float four_me = (float)(4. * ME);
     if (qf < four_me * 0.99999f)
         return false;
-    if (!(qf > four_me * 1.00001f) && q <= 4. * ME)
-        return false;
     const float shift = fpconv::f32(c.pp_kmax_shift);
     const float ub = Kf + shift, margin = 1e-5f * (Kf + fabsf(shift));
     if (qf >= ub + margin)
         return false;
-    if (!(qf <= ub - margin) && q >= K + c.pp_kmax_shift)
-        return false;
+    if (!(qf > four_me * 1.00001f) || !(qf <= ub - margin))
+        return pprod_live_exact(K, q, c.mass, c.pp_kmax_shift, c.inv_mass_h, c.inv_mass_l);
     // argmin in float, with K - q (gamma - q/m = 1 + (K - q)/m) as a
     // float-float difference; the reference's IEEE value decides only within
     // 1e-5 of a bound

@@ -3,10 +3,11 @@
  * caller's stream.
  *
  *  1. classify: per pair, the kinematic bounds decided as the FP64 kernels
- *     decide them (closed -> 0), the normalised features and the trust-grid
- *     cell.  Pairs inside the trained domain whose cell passed the held-out
- *     error check go to the network list; the others to the fallback list
- *     (both in the model's scratch, appended with warp-aggregated atomics).
+ *     decide them (closed -> 0); for the open pairs, compacted in shared
+ *     memory, the normalised features and the trust-grid cell.  Pairs inside
+ *     the trained domain whose cell passed the held-out error check go to the
+ *     network list; the others to the fallback list (both in the model's
+ *     scratch, positions from block-wide scans).
  *     Then netprep: the float baseline of mlp.cuh for each listed pair,
  *     densely over the list.
  *  2. network (tcgen05): a persistent CTA of four warpgroups keeps two tiles
@@ -71,7 +72,7 @@ struct InferParams {
     float Zf[MAX_EL];
     Norm norm;
     const uint8_t *trust;  // [n_seg][64][64]
-    float logk_lo, logk_span, lognu_lo, lognu_span;
+    float logk_lo, logk_scale, lognu_lo, lognu_scale;  // cell = floor((log - lo) * scale)
     // lists
     int32_t *net_idx;
     float *net_base;
@@ -93,104 +94,149 @@ __device__ __forceinline__ void append(unsigned long long *counter, bool flag, i
     slot = flag ? (int)(base + __popc(m & ((1u << lane) - 1u))) : -1;
 }
 
-// Classify, in tiles of 256 x CL_ITEMS pairs: the list positions come from a
-// block-wide scan and one atomicAdd per list per tile (one per warp, with
-// every warp of the grid on the same two counters, serialised in L2 and
-// took most of this kernel's time).
-constexpr int CL_THREADS = 256, CL_ITEMS = 4;
+// Classify, in tiles of CL_TILE pairs, in two phases.
+//  1. Bounds: each thread decides the kinematic bounds of CL_ITEMS pairs as
+//     the FP64 kernels decide them (open_fast), writes 0 for a closed pair,
+//     and the open pairs (index, segment, K, q) are compacted into a
+//     shared-memory queue (block-wide scan).
+//  2. Features, densely over the queue: log K, log(q / (K + m)) (fast float
+//     logs; the network's inputs need ~1e-6), the trust-grid cell (by
+//     multiplication with the grid scale, as the host's cell assignment) and
+//     its trust bit; trusted pairs go to the network list, the others to the
+//     fallback list, with list positions from a block-wide scan and one
+//     atomicAdd per list per tile.
+// Only open pairs (20% for photonuclear, 54% for pair production on the
+// benchmark law) pay for features.
+constexpr int CL_THREADS = 256, CL_ITEMS = 4, CL_TILE = CL_THREADS * CL_ITEMS;
+
+// Exclusive block-wide scan of two counts (256 threads); returns this
+// thread's offsets and writes the totals to *tot_a, *tot_b (shared).
+__device__ __forceinline__ void block_scan2(int ca, int cb, int &oa, int &ob, int *wa, int *wb, int *tot_a,
+                                            int *tot_b) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    int sa = ca, sb = cb;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const int ya = __shfl_up_sync(0xffffffffu, sa, o), yb = __shfl_up_sync(0xffffffffu, sb, o);
+        if (lane >= o) {
+            sa += ya;
+            sb += yb;
+        }
+    }
+    if (lane == 31) {
+        wa[warp] = sa;
+        wb[warp] = sb;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int ta = 0, tb = 0;
+        for (int w = 0; w < CL_THREADS / 32; w++) {
+            const int x = wa[w], y = wb[w];
+            wa[w] = ta;
+            wb[w] = tb;
+            ta += x;
+            tb += y;
+        }
+        *tot_a = ta;
+        *tot_b = tb;
+    }
+    __syncthreads();
+    oa = wa[warp] + sa - ca;
+    ob = wb[warp] + sb - cb;
+}
 
 template <int PROC>
 __global__ void __launch_bounds__(CL_THREADS) classify_kernel(const __grid_constant__ InferParams p) {
-    __shared__ int warp_n[CL_THREADS / 32], warp_f[CL_THREADS / 32];
+    __shared__ int warp_a[CL_THREADS / 32], warp_b[CL_THREADS / 32];
+    __shared__ int tot_a, tot_b;
     __shared__ unsigned long long base_n, base_f;
-    __shared__ float4 s_feat[CL_ITEMS][CL_THREADS];  // the items stay rolled (one copy of the bound checks)
-    __shared__ uint8_t s_seg[CL_ITEMS][CL_THREADS];
+    __shared__ double qK[CL_TILE], qq[CL_TILE];  // the open pairs of the tile
+    __shared__ int32_t qi[CL_TILE];
+    __shared__ uint8_t qs[CL_TILE];
+    __shared__ float4 s_feat[CL_ITEMS][CL_THREADS];
     const int64_t n = p.seg_begin[p.n_seg];
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     int seg_at = 0;  // segment of this thread's last pair
-    for (int64_t tile = (int64_t)blockIdx.x * CL_THREADS * CL_ITEMS; tile < n;
-         tile += (int64_t)gridDim.x * CL_THREADS * CL_ITEMS) {
-        unsigned net_mask = 0, fb_mask = 0;
-#pragma unroll 1
+    for (int64_t tile = (int64_t)blockIdx.x * CL_TILE; tile < n; tile += (int64_t)gridDim.x * CL_TILE) {
+        // phase 1: bounds; closed pairs get 0, open pairs are queued
+        unsigned open_mask = 0, seg_bits = 0;  // segment of item j in bits 4j .. 4j + 3 (n_seg <= 16)
+#pragma unroll 1  // one copy of the bound checks
         for (int j = 0; j < CL_ITEMS; j++) {
             const int64_t i = tile + j * CL_THREADS + threadIdx.x;
-            float4 f = make_float4(0.f, 0.f, 0.f, 0.f);
-            int seg = seg_at;
             if (i < n) {
-                // a thread's pairs come in increasing order: resume the search
+                int seg = seg_at;  // a thread's pairs come in increasing order: resume the search
                 while (seg + 1 < p.n_seg && i >= p.seg_begin[seg + 1])
                     seg++;
                 seg_at = seg;
-                const noa_dcs_consts &c = p.consts[seg];
-                const double K = p.K[i], q = p.q[i];
-                const bool open = open_fast<PROC>(K, q, c);
-                // the cell and the features for every pair (few instructions,
-                // no divergence); only the trust lookup and the stores branch
-                const float Kf = fpconv::f32(K);
-                const float lk = logf(Kf), ln = logf(fpconv::f32(q) / (Kf + c.mass_h));
-                const float fk = floorf((lk - p.logk_lo) / p.logk_span * 64.f);
-                const float fn = floorf((ln - p.lognu_lo) / p.lognu_span * 64.f);
+                if (open_fast<PROC>(p.K[i], p.q[i], p.consts[seg])) {
+                    open_mask |= 1u << j;
+                    seg_bits |= (unsigned)seg << (4 * j);
+                } else {
+                    p.out[i] = 0.;
+                }
+            }
+        }
+        int at, unused;
+        block_scan2(__popc(open_mask), 0, at, unused, warp_a, warp_b, &tot_a, &tot_b);
+        const int n_open = tot_a;
+#pragma unroll
+        for (int j = 0; j < CL_ITEMS; j++) {
+            if (open_mask & (1u << j)) {
+                const int64_t i = tile + j * CL_THREADS + threadIdx.x;
+                qi[at] = (int32_t)i;
+                qs[at] = (uint8_t)((seg_bits >> (4 * j)) & 15u);
+                qK[at] = p.K[i];  // read in phase 1 by this thread: an L1 hit
+                qq[at] = p.q[i];
+                at++;
+            }
+        }
+        __syncthreads();
+        // phase 2: features, cell and trust of the queued pairs
+        unsigned net_mask = 0, fb_mask = 0;
+#pragma unroll 1
+        for (int j = 0; j < CL_ITEMS; j++) {
+            const int e = j * CL_THREADS + threadIdx.x;
+            if (e < n_open) {
+                const int seg = qs[e];
+                const float Kf = fpconv::f32(qK[e]), qf = fpconv::f32(qq[e]);
+                const float lk = __logf(Kf), ln = __logf(__fdividef(qf, Kf + p.consts[seg].mass_h));
+                const float fk = floorf((lk - p.logk_lo) * p.logk_scale);
+                const float fn = floorf((ln - p.lognu_lo) * p.lognu_scale);
                 const bool in_grid = fk >= 0.f && fk < 64.f && fn >= 0.f && fn < 64.f;
-                const bool trusted = open && in_grid && p.trust[(seg * 64 + (int)fk) * 64 + (int)fn] != 0;
+                const bool trusted = in_grid && p.trust[(seg * 64 + (int)fk) * 64 + (int)fn] != 0;
+                float4 f;
                 f.x = (lk - p.norm.in_shift[0]) * p.norm.in_scale[0];
                 f.y = (ln - p.norm.in_shift[1]) * p.norm.in_scale[1];
                 f.z = (p.Zf[seg] * 0.01f - p.norm.in_shift[2]) * p.norm.in_scale[2];
                 f.w = (p.logA[seg] - p.norm.in_shift[3]) * p.norm.in_scale[3];
-                if (!open)
-                    p.out[i] = 0.;
+                s_feat[j][threadIdx.x] = f;
                 net_mask |= (unsigned)trusted << j;
-                fb_mask |= (unsigned)(open && !trusted) << j;
-            }
-            s_feat[j][threadIdx.x] = f;
-            s_seg[j][threadIdx.x] = (uint8_t)seg;
-        }
-        // block-wide exclusive scan of the two counts
-        const int cn = __popc(net_mask), cf = __popc(fb_mask);
-        int sn = cn, sf = cf;
-#pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-            const int yn = __shfl_up_sync(0xffffffffu, sn, o), yf = __shfl_up_sync(0xffffffffu, sf, o);
-            if (lane >= o) {
-                sn += yn;
-                sf += yf;
+                fb_mask |= (unsigned)!trusted << j;
             }
         }
-        if (lane == 31) {
-            warp_n[warp] = sn;
-            warp_f[warp] = sf;
-        }
-        __syncthreads();
+        int pn, pf;
+        block_scan2(__popc(net_mask), __popc(fb_mask), pn, pf, warp_a, warp_b, &tot_a, &tot_b);
         if (threadIdx.x == 0) {
-            int tn = 0, tf = 0;
-            for (int w = 0; w < CL_THREADS / 32; w++) {
-                const int a = warp_n[w], b = warp_f[w];
-                warp_n[w] = tn;
-                warp_f[w] = tf;
-                tn += a;
-                tf += b;
-            }
-            base_n = tn ? atomicAdd(&p.counters[0], (unsigned long long)tn) : 0ull;
-            base_f = tf ? atomicAdd(&p.counters[1], (unsigned long long)tf) : 0ull;
+            base_n = tot_a ? atomicAdd(&p.counters[0], (unsigned long long)tot_a) : 0ull;
+            base_f = tot_b ? atomicAdd(&p.counters[1], (unsigned long long)tot_b) : 0ull;
         }
         __syncthreads();
-        unsigned long long pn = base_n + (unsigned long long)(warp_n[warp] + sn - cn);
-        unsigned long long pf = base_f + (unsigned long long)(warp_f[warp] + sf - cf);
+        unsigned long long wn = base_n + (unsigned long long)pn, wf = base_f + (unsigned long long)pf;
 #pragma unroll
         for (int j = 0; j < CL_ITEMS; j++) {
-            const int32_t i = (int32_t)(tile + j * CL_THREADS + threadIdx.x);
+            const int e = j * CL_THREADS + threadIdx.x;
             if (net_mask & (1u << j)) {
-                p.net_idx[pn] = i;
-                p.net_feat[pn] = s_feat[j][threadIdx.x];
-                p.net_seg[pn] = s_seg[j][threadIdx.x];
-                pn++;
+                p.net_idx[wn] = qi[e];
+                p.net_feat[wn] = s_feat[j][threadIdx.x];
+                p.net_seg[wn] = qs[e];
+                wn++;
             }
             if (fb_mask & (1u << j)) {
-                p.fb_idx[pf] = i;
-                p.fb_seg[pf] = s_seg[j][threadIdx.x];
-                pf++;
+                p.fb_idx[wf] = qi[e];
+                p.fb_seg[wf] = qs[e];
+                wf++;
             }
         }
-        __syncthreads();  // warp_n / warp_f and the bases are rewritten by the next tile
+        __syncthreads();  // the queue, the scan words and the bases are rewritten by the next tile
     }
 }
 
@@ -628,10 +674,13 @@ extern "C" int noa_dcs_mlp_infer(noa_dcs_mlp *model, const uint8_t *trust, int n
         return NOA_DCS_SUCCESS;
     memcpy(&p.norm, norm, sizeof p.norm);
     p.trust = trust;
+    // the trust grid's cells: 64 x 64 over log K in [log 1e-3, log 1e6] and
+    // log(q / (K + m)) in [log 1e-7, 0], the host's cell assignment
+    // (surrogate.cells) in the same float arithmetic
     p.logk_lo = (float)log(1e-3);
-    p.logk_span = (float)(log(1e6) - log(1e-3));
+    p.logk_scale = (float)(64.0 / (log(1e6) - log(1e-3)));
     p.lognu_lo = (float)log(1e-7);
-    p.lognu_span = (float)(0.0 - log(1e-7));
+    p.lognu_scale = (float)(64.0 / (0.0 - log(1e-7)));
     p.tol = tolerance;
     // scratch: counters, then the two lists
     int dev = 0;

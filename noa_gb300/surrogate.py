@@ -208,10 +208,14 @@ class Surrogate:
 
     # ------------------------------------------------------------ trust grid
     def cells(self, Xraw, elem):
-        """Trust-grid cell of each sample (raw features), -1 outside the trained domain."""
-        lk, ln = Xraw[:, 0], Xraw[:, 1]
-        ik = ((lk - LOGK_RANGE[0]) / (LOGK_RANGE[1] - LOGK_RANGE[0]) * GRID[0]).floor().long()
-        inu = ((ln - LOGNU_RANGE[0]) / (LOGNU_RANGE[1] - LOGNU_RANGE[0]) * GRID[1]).floor().long()
+        """Trust-grid cell of each sample (raw features), -1 outside the
+        trained domain: floor((log - lo) * scale) per axis in float32 with lo
+        and scale rounded to float32, the arithmetic of the inference kernel."""
+        lk, ln = Xraw[:, 0].float(), Xraw[:, 1].float()
+        k_lo, k_sc = float(np.float32(LOGK_RANGE[0])), float(np.float32(GRID[0] / (LOGK_RANGE[1] - LOGK_RANGE[0])))
+        n_lo, n_sc = float(np.float32(LOGNU_RANGE[0])), float(np.float32(GRID[1] / (LOGNU_RANGE[1] - LOGNU_RANGE[0])))
+        ik = ((lk - k_lo) * k_sc).floor().long()
+        inu = ((ln - n_lo) * n_sc).floor().long()
         inside = (ik >= 0) & (ik < GRID[0]) & (inu >= 0) & (inu < GRID[1])
         c = (elem.long() * GRID[0] + ik.clamp(0, GRID[0] - 1)) * GRID[1] + inu.clamp(0, GRID[1] - 1)
         return torch.where(inside, c, torch.full_like(c, -1))
