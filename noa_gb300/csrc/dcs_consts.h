@@ -85,6 +85,8 @@ typedef struct noa_dcs_consts {
     float mass_h, mass_l;          /* mass */
     float io_cm_h, io_cm_l;        /* (mass + me)^2: W_max = 2 me K (K + 2 mass) / ((mass + me)^2 + 2 me K) */
     float mass2_f;                 /* mass^2 rounded to float */
+    float pp_kmax_shift_f;         /* pp_kmax_shift rounded to float */
+    float ph_q_min_f;              /* ph_q_min rounded to float */
 } noa_dcs_consts;
 
 /* Fills c from (A, I, Z, mass) with the reference's expressions (host code;
@@ -128,6 +130,7 @@ static inline void noa_dcs_fill_consts(noa_dcs_consts *c, double A, double I, in
         const double Z13 = pow((double)Z, 1. / 3.);
         c->pp_Z13 = Z13;
         c->pp_kmax_shift = mass * (1. - 0.75 * sqrte * Z13);
+        c->pp_kmax_shift_f = (float)c->pp_kmax_shift;
         const double r = mass / me;
         c->pp_r = r;
         const double A_ = (Z == 1) ? 202.4 : 183.;
@@ -148,6 +151,7 @@ static inline void noa_dcs_fill_consts(noa_dcs_consts *c, double A, double I, in
         c->ph_logA = log(A);
         c->ph_a_low = exp(-0.1 * log(A));
         c->ph_q_min = mpi * (1.0 + 0.5 * mpi / M);
+        c->ph_q_min_f = (float)c->ph_q_min;
         c->ph_log_q02 = log(0.52544 / 0.06527);
         c->ph_inv_log_q02 = 1. / c->ph_log_q02;
         c->ph_scale = 0.5 * 2.603096E-35 * c->scale_A;

@@ -127,7 +127,8 @@ static __device__ __noinline__ bool pprod_live_exact(double K, double q, double 
 }
 
 __device__ __forceinline__ bool pprod_live(double K, double q, const noa_dcs_consts &c) {
-    const float Kf = fpconv::f32(K), qf = fpconv::f32(q);
+    // NaN outside the normal float range: the range test below fails there
+    const float Kf = fpconv::f32_normal(K), qf = fpconv::f32_normal(q);
     if (!(Kf > 1e-20f && Kf < 1e30f && qf > 1e-20f && qf < 1e30f))  // outside the float-safe range (and NaN)
         return pprod_live_exact(K, q, c.mass, c.pp_kmax_shift, c.inv_mass_h, c.inv_mass_l);
     // q <= 4 me and q >= K + m (1 - 0.75 sqrt(e) Z^1/3) (dcs.hh:151-156) in
@@ -135,7 +136,7 @@ __device__ __forceinline__ bool pprod_live(double K, double q, const noa_dcs_con
     constexpr float four_me = (float)(4. * ME);
     if (qf < four_me * 0.99999f)
         return false;
-    const float shift = fpconv::f32(c.pp_kmax_shift);
+    const float shift = c.pp_kmax_shift_f;
     const float ub = Kf + shift, margin = 1e-5f * (Kf + fabsf(shift));
     if (qf >= ub + margin)
         return false;
@@ -145,7 +146,7 @@ __device__ __forceinline__ bool pprod_live(double K, double q, const noa_dcs_con
     // float-float difference; the reference's IEEE value decides only within
     // 1e-5 of a bound
     const FF kmq = ff_add(ff_split(K), ff_neg(ff_split(q)));
-    const float im = fpconv::f32(c.inv_mass);
+    const float im = c.inv_mass_h;
     const float x0 = four_me * lean64::rcp_approx(qf);
     const float gamma = 1.f + Kf * im;
     const float x1 = 6.f * lean64::rcp_approx(gamma * (1.f + (kmq.h + kmq.l) * im));
@@ -236,15 +237,16 @@ __device__ __forceinline__ double pprod_fp64(double K, double q, const noa_dcs_c
 // outside the float-safe range (zero, NaN, inf, huge), take the exact IEEE
 // check.  Only the closed / open answer is taken from float, never a value.
 __device__ __forceinline__ bool photo_live(double K, double q, const noa_dcs_consts &c) {
-    const float Kf = fpconv::f32(K), qf = fpconv::f32(q);
+    // NaN outside the normal float range: the range test below fails there
+    const float Kf = fpconv::f32_normal(K), qf = fpconv::f32_normal(q);
     if (Kf >= 1e-30f && Kf <= 1e30f && qf >= 1e-30f && qf <= 1e30f) {
         constexpr float lo = 0.99999f, hi = 1.00001f;
-        const float qmin = fpconv::f32(c.ph_q_min), cut = 2E-03f * Kf;
+        const float qmin = c.ph_q_min_f, cut = 2E-03f * Kf;
         if (qf < lo || qf < cut * lo || qf > Kf * hi || qf < qmin * lo)
             return false;  // q < 1, q < 2e-3 K, q >= E - m (= K to an ulp), q <= q_min
         if (!(qf < hi || qf < cut * hi || qf > Kf * lo || qf < qmin * hi)) {
-            const float m = fpconv::f32(c.mass);
-            const float Ef = Kf + m, Emq = fpconv::f32(K + c.mass - q);  // q < K (1 - 1e-5): no cancellation
+            const float m = c.mass_h;
+            const float Ef = Kf + m, Emq = fpconv::f32_normal(K + c.mass - q);  // q < K (1 - 1e-5): no cancellation
             const float y = qf / Ef, omy = Emq / Ef;
             const float Q2min = m * m * y * y / omy;
             const float Q2max = (float)(2.0 * PH_M) * (qf - qmin);

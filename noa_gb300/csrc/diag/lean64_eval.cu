@@ -29,7 +29,8 @@ __global__ void lean64_eval_kernel(int fn, const double *__restrict__ x, const d
         case 5: r = fpconv::f64(fpconv::f32(a)); break;      // (double)(float)a
         case 6: r = fpconv::f64i(__double2int_rz(a)); break;  // (double)(int)a
         case 7: r = noa_dcs::ff_to_double(noa_dcs::ff_exp(noa_dcs::ff_from(a))); break;
-        default: r = noa_dcs::ff_to_double(noa_dcs::ff_log(noa_dcs::ff_from(a))); break;
+        case 8: r = noa_dcs::ff_to_double(noa_dcs::ff_log(noa_dcs::ff_from(a))); break;
+        default: r = fpconv::f64(fpconv::f32_normal(a)); break;  // (double)(float)a or NaN
         }
         out[i] = r;
     }
@@ -38,7 +39,7 @@ __global__ void lean64_eval_kernel(int fn, const double *__restrict__ x, const d
 } // namespace
 
 extern "C" int noa_dcs_lean64_eval(int fn, const double *x, const double *y, double *out, int64_t n, void *stream) {
-    if (fn < 0 || fn > 8 || n < 0 || (n > 0 && (!x || !out || (fn == 3 && !y))))
+    if (fn < 0 || fn > 9 || n < 0 || (n > 0 && (!x || !out || (fn == 3 && !y))))
         return NOA_DCS_ERROR_INVALID_VALUE;
     if (n == 0)
         return NOA_DCS_SUCCESS;

@@ -25,8 +25,10 @@ int noa_dcs_probe_fma(int fp64, void *out, int blocks, int iters, double *flops,
  * 4 sqrt -- of its integer-pipe conversions -- fn 5 (double)(float)x,
  * 6 (double)(int)x for x in int range -- or of its float-float functions on x
  * split into a float pair -- fn 7 exp (-87 < x < 88), 8 log (x > 0, normal
- * float range) -- on device buffers, so that their error can be measured
- * against a reference libm and the conversions checked against the casts. */
+ * float range) -- or fn 9 the normal-range conversion (double)(float)x, NaN
+ * outside the normal float range, on device buffers, so that their error can
+ * be measured against a reference libm and the conversions checked against
+ * the casts. */
 int noa_dcs_lean64_eval(int fn, const double *x, const double *y, double *out, int64_t n, void *stream);
 
 #ifdef __cplusplus

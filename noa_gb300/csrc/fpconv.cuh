@@ -18,6 +18,7 @@
 #include <cuda_runtime.h>
 #endif
 
+#include <cmath>
 #include <cstdint>
 
 #if defined(__CUDACC__)
@@ -84,6 +85,25 @@ NOA_CONV_HD float f32(double x) {
     return __uint_as_float(s | r);
 #else
     return (float)x;
+#endif
+}
+
+// (float)x, round to nearest even, for |x| in the normal float range
+// (exponent 2^-126 .. 2^127; a carry to infinity is the correct result);
+// NaN for every other input (zero, float subnormals, overflow, inf, NaN).
+// Equal to f32 wherever it is not NaN, at a third of its integer
+// operations: for tests that send out-of-range inputs to an exact path.
+NOA_CONV_HD float f32_normal(double x) {
+#if defined(__CUDA_ARCH__)
+    const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+    const unsigned e = (unsigned)(b >> 52) & 0x7FFu;
+    const unsigned long long a = b & 0x7FFFFFFFFFFFFFFFull;
+    const unsigned long long t = a + 0x0FFFFFFFull + ((a >> 29) & 1ull);
+    const unsigned r = ((unsigned)(b >> 32) & 0x80000000u) | ((unsigned)(t >> 29) - (896u << 23));
+    return e - 897u <= 253u ? __uint_as_float(r) : __uint_as_float(0x7FC00000u);
+#else
+    const float f = (float)x;
+    return (std::fabs(x) >= 0x1p-126 && std::fabs(x) < 0x1p128) ? f : NAN;
 #endif
 }
 

@@ -103,9 +103,10 @@ __device__ __forceinline__ bool baseline(double K, double q, const noa_dcs_const
 // rounding); the exact checks decide everything else.
 template <int PROC>
 __device__ __forceinline__ bool surely_closed(double K, double q, const noa_dcs_consts &c) {
-    const float Kf = fpconv::f32(K), qf = fpconv::f32(q);
+    // NaN outside the normal float range: no pair is then "surely closed"
+    const float Kf = fpconv::f32_normal(K), qf = fpconv::f32_normal(q);
     if (PROC == NOA_DCS_PAIR_PRODUCTION)
-        return qf < (float)(4. * noa_dcs::ME) * 0.99999f || qf > (Kf + fpconv::f32(c.pp_kmax_shift)) * 1.00001f;
+        return qf < (float)(4. * noa_dcs::ME) * 0.99999f || qf > (Kf + c.pp_kmax_shift_f) * 1.00001f;
     return qf < 0.99999f || qf < 2E-03f * Kf * 0.99999f;
 }
 

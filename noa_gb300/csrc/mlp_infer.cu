@@ -197,7 +197,7 @@ __global__ void __launch_bounds__(CL_THREADS) classify_kernel(const __grid_const
             const int e = j * CL_THREADS + threadIdx.x;
             if (e < n_open) {
                 const int seg = qs[e];
-                const float Kf = fpconv::f32(qK[e]), qf = fpconv::f32(qq[e]);
+                const float Kf = fpconv::f32_normal(qK[e]), qf = fpconv::f32_normal(qq[e]);  // NaN: no cell
                 const float lk = __logf(Kf), ln = __logf(__fdividef(qf, Kf + p.consts[seg].mass_h));
                 const float fk = floorf((lk - p.logk_lo) * p.logk_scale);
                 const float fn = floorf((ln - p.lognu_lo) * p.lognu_scale);

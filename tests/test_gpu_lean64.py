@@ -101,6 +101,29 @@ def test_integer_pipe_float_conversion_is_the_cast(cuda_device):
     assert np.array_equal(_bits(got[~nan]), _bits(exp[~nan]))
 
 
+def test_normal_range_float_conversion(cuda_device):
+    """fpconv::f32_normal (the bound checks' conversion): exactly the cast
+    (double)(float)x for |x| in [2^-126, 2^128), including ties, carries into
+    the exponent and to infinity; NaN for every other input (zeros, float
+    subnormals, larger values, infinities, NaN), so that range tests fail."""
+    rng = np.random.default_rng(9)
+    raw = rng.integers(0, 1 << 63, 400_000, dtype=np.uint64).view(np.float64)
+    wide = rng.standard_normal(200_000) * 10.0 ** rng.uniform(-50, 45, 200_000)
+    f = (rng.standard_normal(50_000) * 10.0 ** rng.uniform(-37, 38, 50_000)).astype(np.float32).astype(np.float64)
+    fb = f.view(np.uint64)
+    ties = np.concatenate([fb + (1 << 28), fb - (1 << 28), fb + (1 << 28) + 1]).view(np.float64)
+    special = np.array([0.0, -0.0, np.inf, -np.inf, np.nan, 1e-45, 1.1754943508222875e-38, 1.1754942e-38,
+                        2.0 ** -126, -(2.0 ** -126), 2.0 ** 128, np.nextafter(2.0 ** 128, 0), 3.4028235e38, 1e300])
+    x = np.concatenate([raw, wide, ties, special])
+    got = run(9, x)
+    ax = np.abs(x)
+    normal = (ax >= 2.0 ** -126) & (ax < 2.0 ** 128)
+    with np.errstate(over="ignore", invalid="ignore"):
+        exp = x.astype(np.float32).astype(np.float64)
+    assert np.all(np.isnan(got[~normal]))
+    assert np.array_equal(_bits(got[normal]), _bits(exp[normal]))
+
+
 def test_integer_pipe_int_conversion_is_the_cast(cuda_device):
     rng = np.random.default_rng(8)
     i = np.concatenate([rng.integers(-(1 << 31), 1 << 31, 200_000), [0, 1, -1, 2**31 - 1, -2**31, 1023, -1074]])
