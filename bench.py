@@ -546,7 +546,8 @@ def time_surrogate(torch, args):
         return s.elapsed_time(e) * 1e-3 / steps
 
     for p, name in ((1, "pair_production"), (2, "photonuclear")):
-        sur = train_recipe(p, n_valid=6_000_000, steps1=30_000, steps2=90_000, batch=8192, heldout=2_000_000)
+        # trained on 2e7 plain-kernel samples over the 10 elements
+        sur = train_recipe(p, n_valid=20_000_000, steps1=30_000, steps2=90_000, batch=8192, heldout=2_000_000)
         ref = torch.empty_like(tk)
         out = torch.empty_like(tk)
         entry = {"training": sur.info}
@@ -562,6 +563,10 @@ def time_surrogate(torch, args):
             _, st = sur.infer(tk, tq, counts, out=out)
             stats.update(st)
         entry["surrogate_s"] = timed(run)
+        # the same pipeline with every cell untrusted: what the network adds
+        none = np.zeros_like(sur.trust)
+        entry["no_network_s"] = timed(lambda: sur.infer(tk, tq, counts, trust=none, out=out))
+        sur.infer(tk, tq, counts, out=out)
         nz = ref != 0
         rel = ((out[nz] - ref[nz]).abs() / ref[nz]).float()
         entry.update({
@@ -569,6 +574,7 @@ def time_surrogate(torch, args):
                             "surrogate": nq / entry["surrogate_s"]},
             "speedup_vs_fp64": entry["fp64_s"] / entry["surrogate_s"],
             "speedup_vs_fp32c": entry["fp32c_s"] / entry["surrogate_s"],
+            "speedup_vs_no_network": entry["no_network_s"] / entry["surrogate_s"],
             "network_share_of_open": stats["network"] / max(1, int(nz.sum())),
             "status": stats["status"],
             "max_rel": float(rel.max()), "median_rel": float(rel.median()),
@@ -811,6 +817,7 @@ def summarise(line):
     sg = line.get("surrogate")
     if sg:
         s["surrogate"] = {k: {"x_fp64": _r(v["speedup_vs_fp64"], 3), "x_fp32c": _r(v["speedup_vs_fp32c"], 3),
+                              "x_no_net": _r(v.get("speedup_vs_no_network"), 3),
                               "max": _r(v["max_rel"], 2), "above_1e-3": v["frac_above_1e-3"],
                               "net_share": _r(v["network_share_of_open"], 2),
                               "train_s": _r(v["training"].get("train_seconds"), 3)}

@@ -159,7 +159,16 @@ __global__ void __launch_bounds__(CL_THREADS) classify_kernel(const __grid_const
     for (int64_t tile = (int64_t)blockIdx.x * CL_TILE; tile < n; tile += (int64_t)gridDim.x * CL_TILE) {
         // phase 1: bounds; closed pairs get 0, open pairs are queued
         unsigned open_mask = 0, seg_bits = 0;  // segment of item j in bits 4j .. 4j + 3 (n_seg <= 16)
-#pragma unroll 1  // one copy of the bound checks
+        // the tile's K and q are all requested before the first decision
+        // (memory latency, not arithmetic, bounds this phase)
+        double Kv[CL_ITEMS], qv[CL_ITEMS];
+#pragma unroll
+        for (int j = 0; j < CL_ITEMS; j++) {
+            const int64_t i = tile + j * CL_THREADS + threadIdx.x;
+            Kv[j] = i < n ? p.K[i] : 0.;
+            qv[j] = i < n ? p.q[i] : 0.;
+        }
+#pragma unroll
         for (int j = 0; j < CL_ITEMS; j++) {
             const int64_t i = tile + j * CL_THREADS + threadIdx.x;
             if (i < n) {
@@ -167,7 +176,7 @@ __global__ void __launch_bounds__(CL_THREADS) classify_kernel(const __grid_const
                 while (seg + 1 < p.n_seg && i >= p.seg_begin[seg + 1])
                     seg++;
                 seg_at = seg;
-                if (open_fast<PROC>(p.K[i], p.q[i], p.consts[seg])) {
+                if (open_fast<PROC>(Kv[j], qv[j], p.consts[seg])) {
                     open_mask |= 1u << j;
                     seg_bits |= (unsigned)seg << (4 * j);
                 } else {
@@ -184,15 +193,15 @@ __global__ void __launch_bounds__(CL_THREADS) classify_kernel(const __grid_const
                 const int64_t i = tile + j * CL_THREADS + threadIdx.x;
                 qi[at] = (int32_t)i;
                 qs[at] = (uint8_t)((seg_bits >> (4 * j)) & 15u);
-                qK[at] = p.K[i];  // read in phase 1 by this thread: an L1 hit
-                qq[at] = p.q[i];
+                qK[at] = Kv[j];
+                qq[at] = qv[j];
                 at++;
             }
         }
         __syncthreads();
         // phase 2: features, cell and trust of the queued pairs
         unsigned net_mask = 0, fb_mask = 0;
-#pragma unroll 1
+#pragma unroll
         for (int j = 0; j < CL_ITEMS; j++) {
             const int e = j * CL_THREADS + threadIdx.x;
             if (e < n_open) {

@@ -1,7 +1,8 @@
 """GPU tests of the surrogate's inference (noa_dcs_mlp_infer): the tcgen05
-network kernel against the validated tensor-core forward (mma.sync path),
-the trust grid and the FP32C fallback against the oracle, and what the
-trained network gains over the kernels without it."""
+network kernel against the training path's forward, the trust grid and the
+FP32C fallback against the oracle, and what the trained surrogate gains over
+the kernels without it (plain FP64, the FP32C engine, and its own pipeline
+with the network switched off)."""
 import numpy as np
 import pytest
 import torch
@@ -38,8 +39,9 @@ def oracle_all(process, K, q):
 
 
 def test_tcgen05_network_matches_reference_forward(trained):
-    """All cells trusted: every open pair goes through the tcgen05 kernel; its
-    result equals exp(baseline + residual) of the mma.sync forward."""
+    """All cells trusted: every open pair goes through the tcgen05 inference
+    kernel; its result equals exp(baseline + residual) of the training
+    path's forward (noa_dcs_mlp_predict)."""
     s = trained
     tk, tq, K, q = queries()
     ones = np.ones((len(BATCH_Z), *GRID), dtype=np.uint8)
@@ -74,10 +76,12 @@ def test_trusted_inference_within_bound(trained):
     nz = exp != 0
     rel = np.abs(got[nz] - exp[nz]) / exp[nz]
     print(s.process, st, "frac>1e-3", float((rel > 1e-3).mean()), "max", float(rel.max()), s.info)
-    # the network answers a real share (the short test recipe trusts ~7-8% of the
-    # open pairs at the production criterion; the bench's longer recipe 25-40%)
+    # the network answers a real share (the short test recipe trusts ~6% of the
+    # open pairs; the bench's longer recipe 14-21%)
     assert st["network"] > 0.04 * nz.sum()
-    assert float((rel > 1e-3).mean()) < 2e-3     # held-out-trusted cells generalise
+    # no query above the bound: the lattice and held-out checks of the trust
+    # grid keep every trusted cell within it
+    assert float(rel.max()) <= 1e-3, float(rel.max())
     assert float(np.median(rel)) < 1e-4
     # into a caller buffer: the same bits
     buf = torch.full_like(tk, -7.0)
@@ -129,3 +133,48 @@ def test_surrogate_gains_over_plain_fp64(trained):
     assert float(((got[nz] - ref[nz]).abs() / ref[nz]).max()) < 1e-3
     print(s.process, "fp64 ms", t64, "surrogate ms", tsur)
     assert tsur * 2 < t64
+
+
+def test_surrogate_against_fp32c_and_without_the_network(trained):
+    """The same 4e6 queries through (a) the surrogate, (b) the FP32C batched
+    engine and (c) the surrogate's pipeline with every cell untrusted (no
+    network).  Timings are reported; asserted: every path within its bound,
+    and the surrogate path not slower than the FP32C engine for pair
+    production (its list structure -- bounds decided once, a dense fallback
+    list -- is cheaper than the engine's per-tile queues; the network itself
+    costs more per pair than the FP32C fallback on GB300, which the bench
+    reports as speedup_vs_no_network)."""
+    from noa_gb300.batched import BatchPlan
+    s = trained
+    counts = [400_000] * len(BATCH_Z)
+    K, q = batch_inputs(BATCH_Z, counts, seed=99)
+    tk, tq = torch.from_numpy(K).cuda(), torch.from_numpy(q).cuda()
+    none = np.zeros((len(BATCH_Z), *GRID), dtype=np.uint8)
+
+    def timed(fn, reps=5):
+        fn()
+        torch.cuda.synchronize()
+        ts = []
+        for _ in range(reps):
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record()
+            fn()
+            b.record()
+            torch.cuda.synchronize()
+            ts.append(a.elapsed_time(b))
+        return sorted(ts)[len(ts) // 2]
+
+    out32 = torch.empty_like(tk)
+    with BatchPlan(s.process, [ELEMENTS[z] for z in BATCH_Z], counts, MUON_MASS, "fp32c") as plan:
+        plan.set_tile(256, 8, 2)
+        t32 = timed(lambda: plan.execute(out32, tk, tq))
+    buf = torch.empty_like(tk)
+    tsur = timed(lambda: s.infer(tk, tq, counts, out=buf))
+    got, st = s.infer(tk, tq, counts)
+    tnone = timed(lambda: s.infer(tk, tq, counts, trust=none, out=buf))
+    print(s.process, "fp32c engine ms", t32, "surrogate ms", tsur, "without network ms", tnone, st)
+    nz = out32 != 0
+    assert torch.equal(got == 0, out32 == 0)
+    assert float(((got[nz] - out32[nz]).abs() / out32[nz]).max()) < 1.01e-3
+    if s.process == 1:
+        assert tsur < t32, (tsur, t32)
