@@ -362,10 +362,15 @@ def train_recipe(process, n_valid=10_000_000, steps1=60_000, steps2=150_000, bat
     worst.scatter_reduce_(0, cell[k], err[k], reduce="amax")
     tc = s.cells(Xv, ev)
     keep = (tc >= 0) & (worst[tc.clamp(min=0)] <= keep_err)
-    s.fit(X[keep].contiguous(), T[keep].contiguous(), steps=steps2, lr=5e-4, lr_final=5e-6, seed=seed + 1)
+    # stage 2 needs at least one batch of kept samples (a very short stage 1
+    # can leave fewer); without them the model stays as stage 1 left it
+    if int(keep.sum()) >= s.batch:
+        s.fit(X[keep].contiguous(), T[keep].contiguous(), steps=steps2, lr=5e-4, lr_final=5e-6, seed=seed + 1)
+    else:
+        steps2 = 0
     info = s.build_trust(Xh, Rh, vh, eht, bound=bound, open_zero=zh)
     info.update({"train_seconds": time.time() - t0, "training_pairs": int(Xv.shape[0]),
-                 "stage2_pairs": int(keep.sum()), "steps": steps1 + steps2, "batch": batch})
+                 "stage2_pairs": int(keep.sum()) if steps2 else 0, "steps": steps1 + steps2, "batch": batch})
     if log:
         log(info)
     s.info = info
@@ -377,12 +382,17 @@ def _main(argv=None):
 
         python -m noa_gb300.surrogate train PROCESS OUT.npz [--pairs N] [--steps1 S] [--steps2 S]
         python -m noa_gb300.surrogate infer MODEL.npz [--queries N] [--repeat R]
-    """
+                                         [--trust model|all|none] [--fp32c]
+
+    infer evaluates N seeded queries over the model's elements (equal
+    counts); --trust all sends every open pair to the network and none sends
+    none (the pipeline without the network), model uses the trained trust
+    grid; --fp32c also times the FP32C batched engine on the same queries.
+    Times are CUDA-event milliseconds of one call (the last of R)."""
     import argparse
     import json
-    import time
 
-    from .batched import batch_inputs
+    from .batched import BatchPlan, batch_inputs
     ap = argparse.ArgumentParser(prog="python -m noa_gb300.surrogate")
     sub = ap.add_subparsers(dest="cmd", required=True)
     t = sub.add_parser("train")
@@ -395,6 +405,8 @@ def _main(argv=None):
     i.add_argument("model")
     i.add_argument("--queries", type=float, default=1e7)
     i.add_argument("--repeat", type=int, default=3)
+    i.add_argument("--trust", choices=["model", "all", "none"], default="model")
+    i.add_argument("--fp32c", action="store_true")
     a = ap.parse_args(argv)
     if a.cmd == "train":
         s = train_recipe(a.process, n_valid=int(a.pairs), steps1=a.steps1, steps2=a.steps2)
@@ -407,12 +419,29 @@ def _main(argv=None):
     counts[-1] += nq - sum(counts)
     K, q = batch_inputs(s.elements_z, counts, seed=777)
     tk, tq = torch.from_numpy(K).cuda(), torch.from_numpy(q).cuda()
-    st = {}
-    for _ in range(a.repeat):
-        t0 = time.perf_counter()
-        out, st = s.infer(tk, tq, counts)
-        dt = time.perf_counter() - t0
-    print(json.dumps({"queries": nq, "seconds": dt, "evals_per_s": nq / dt, **st}))
+    del K, q
+    out = torch.empty_like(tk)
+    shape = (len(s.elements_z), *GRID)
+    trust = {"model": None, "all": np.ones(shape, np.uint8), "none": np.zeros(shape, np.uint8)}[a.trust]
+
+    def timed(fn):
+        ms, res = 0.0, None
+        for _ in range(max(1, a.repeat)):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            res = fn()
+            e1.record()
+            torch.cuda.synchronize()
+            ms = e0.elapsed_time(e1)
+        return ms, res
+
+    ms, (_, st) = timed(lambda: s.infer(tk, tq, counts, trust=trust, out=out))
+    line = {"queries": nq, "trust": a.trust, "ms": ms, "evals_per_s": nq / (ms * 1e-3), **st}
+    if a.fp32c:
+        with BatchPlan(s.process, [ELEMENTS[z] for z in s.elements_z], counts, s.mass, "fp32c") as plan:
+            plan.set_tile(256, 8, 2)
+            line["fp32c_engine_ms"], _ = timed(lambda: plan.execute(out, tk, tq))
+    print(json.dumps(line))
 
 
 if __name__ == "__main__":

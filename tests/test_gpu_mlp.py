@@ -123,3 +123,14 @@ def test_short_training_reduces_loss_and_checkpoint_roundtrip(cuda_device, tmp_p
     p1, m1, v1, st1 = s.get_params()
     p2, m2, v2, st2 = s2.get_params()
     assert st1 == st2 == 400 and np.array_equal(p1, p2) and np.array_equal(m1, m2)
+
+
+def test_recipe_with_a_stage_two_smaller_than_a_batch(cuda_device):
+    """A very short first stage can leave fewer kept samples than one batch;
+    the recipe then skips stage 2 (and says so) instead of failing."""
+    from noa_gb300.surrogate import train_recipe
+    s = train_recipe(1, n_valid=200_000, steps1=20, steps2=20, batch=8192, heldout=100_000)
+    assert s.info["steps"] in (20, 40)
+    assert (s.info["stage2_pairs"] == 0) == (s.info["steps"] == 20)
+    assert s.trust is not None
+    s.close()
