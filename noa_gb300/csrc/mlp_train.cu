@@ -36,6 +36,7 @@ using namespace noa_mlp;
 
 namespace {
 
+constexpr int NPARAM_PAD = (NPARAM + 3) & ~3;  // parameter-sized buffers, padded to 16 bytes
 constexpr int G_THREADS = 256;
 constexpr int G_TMEM_COLS = 128;  // the 128 x 128 FP32 accumulator
 using noa_tc::MAT_BYTES;
@@ -194,10 +195,12 @@ __global__ void __launch_bounds__(G_THREADS, 1) mlp_gemm_kernel(const GemmArgs g
             float v[32];
             tmem_ld32(acc + lane_base + (uint32_t)c0, v);
             if (MODE == G_DW) {
-                // row = out index, column = in index
+                // row = out index, column = in index; 16-byte vector atomics
+                // (the weight blocks of G start 16-byte aligned)
 #pragma unroll
-                for (int j = 0; j < 32; j++)
-                    atomicAdd(&g.dW[row * H + c0 + j], v[j]);
+                for (int j = 0; j < 32; j += 4)
+                    atomicAdd(reinterpret_cast<float4 *>(&g.dW[row * H + c0 + j]),
+                              make_float4(v[j], v[j + 1], v[j + 2], v[j + 3]));
             } else if (row0 + row < g.M) {
                 const size_t o = (size_t)(row0 + row) * H + c0;
                 if (MODE == G_FWD) {
@@ -265,11 +268,15 @@ __global__ void __launch_bounds__(128) mlp_out_kernel(const float *__restrict__ 
                                                       float *pred_out) {
     __shared__ float sd[128];
     const int s = blockIdx.x * 128 + threadIdx.x;
+    const int ns = min(128, M - (int)blockIdx.x * 128);  // samples of this CTA
     float dp = 0.f;
     if (s < M) {
-        float y = P[OFF_BO];
+        // four partial sums: the row's loads are independent and overlap
+        float y4[4] = {P[OFF_BO], 0.f, 0.f, 0.f};
+#pragma unroll 8
         for (int k = 0; k < H; k++)
-            y = fmaf(P[OFF_WO + k], H3[(size_t)s * H + k], y);
+            y4[k & 3] = fmaf(P[OFF_WO + k], H3[(size_t)s * H + k], y4[k & 3]);
+        const float y = (y4[0] + y4[1]) + (y4[2] + y4[3]);
         if (pred_out)
             pred_out[s] = y;
         if (T) {
@@ -282,14 +289,18 @@ __global__ void __launch_bounds__(128) mlp_out_kernel(const float *__restrict__ 
     __syncthreads();
     if (!T)
         return;
-    if (s < M)
+    if (s < M) {
+#pragma unroll 8
         for (int k = 0; k < H; k++)
             dZ3[(size_t)s * H + k] = dp * P[OFF_WO + k] * dsilu(Z3[(size_t)s * H + k]);
-    // dWo[k] = sum_s dp_s h3[s][k], thread k
+    }
+    // dWo[k] = sum_s dp_s h3[s][k], thread k (coalesced across threads)
     const int k = threadIdx.x;
-    float g = 0.f;
-    for (int i = 0; i < 128 && blockIdx.x * 128 + i < M; i++)
-        g = fmaf(sd[i], H3[(size_t)(blockIdx.x * 128 + i) * H + k], g);
+    float g4[4] = {0.f, 0.f, 0.f, 0.f};
+#pragma unroll 8
+    for (int i = 0; i < ns; i++)
+        g4[i & 3] = fmaf(sd[i], H3[(size_t)(blockIdx.x * 128 + i) * H + k], g4[i & 3]);
+    const float g = (g4[0] + g4[1]) + (g4[2] + g4[3]);
     atomicAdd(&G[OFF_WO + k], g);
     if (k == 0) {
         float b = 0.f;
@@ -303,16 +314,19 @@ __global__ void __launch_bounds__(128) mlp_out_kernel(const float *__restrict__ 
 __global__ void __launch_bounds__(128) mlp_bwd1_kernel(const float *__restrict__ dZ1, const float *__restrict__ X,
                                                        float *G, int M) {
     const int j = threadIdx.x;
+    const int ns = min(128, M - (int)blockIdx.x * 128);  // samples of this CTA
     float gw[IN] = {0.f, 0.f, 0.f, 0.f}, gb = 0.f;
-    for (int i = 0; i < 128; i++) {
+    // bounds hoisted out of the loop so that the unrolled loads overlap
+#pragma unroll 8
+    for (int i = 0; i < ns; i++) {
         const int s = blockIdx.x * 128 + i;
-        if (s >= M)
-            break;
         const float d = dZ1[(size_t)s * H + j];
+        const float4 x = reinterpret_cast<const float4 *>(X)[s];
         gb += d;
-#pragma unroll
-        for (int c = 0; c < IN; c++)
-            gw[c] = fmaf(d, X[s * IN + c], gw[c]);
+        gw[0] = fmaf(d, x.x, gw[0]);
+        gw[1] = fmaf(d, x.y, gw[1]);
+        gw[2] = fmaf(d, x.z, gw[2]);
+        gw[3] = fmaf(d, x.w, gw[3]);
     }
 #pragma unroll
     for (int c = 0; c < IN; c++)
@@ -576,7 +590,7 @@ int noa_dcs_mlp_create(noa_dcs_mlp **out, int process, int batch) {
         if (e == cudaSuccess)
             e = cudaMalloc((void **)a, act);
     if (e == cudaSuccess)
-        e = cudaMalloc((void **)&m->P, sizeof(float) * NPARAM * 4);
+        e = cudaMalloc((void **)&m->P, sizeof(float) * NPARAM_PAD * 4);
     if (e == cudaSuccess)
         e = cudaMalloc((void **)&m->Wb, sizeof(__nv_bfloat16) * 4 * H * H);
     if (e == cudaSuccess)
@@ -590,13 +604,13 @@ int noa_dcs_mlp_create(noa_dcs_mlp **out, int process, int batch) {
         delete m;
         return mfail(NOA_DCS_ERROR_CUDA, "model allocation", e);
     }
-    m->G = m->P + NPARAM;
-    m->Mm = m->G + NPARAM;
-    m->V = m->Mm + NPARAM;
+    m->G = m->P + NPARAM_PAD;  // each block 16-byte aligned (vector atomics on G)
+    m->Mm = m->G + NPARAM_PAD;
+    m->V = m->Mm + NPARAM_PAD;
     m->Tb = m->Xb + (size_t)batch * IN;
     m->loss = m->Tb + batch;
     m->status = reinterpret_cast<unsigned int *>(m->loss + 1);
-    cudaMemset(m->P, 0, sizeof(float) * NPARAM * 4);
+    cudaMemset(m->P, 0, sizeof(float) * NPARAM_PAD * 4);
     cudaMemset(m->status, 0, sizeof(unsigned int));
     cudaMemset(m->Wb, 0, sizeof(__nv_bfloat16) * 4 * H * H);
     *out = m;
