@@ -178,3 +178,28 @@ def test_surrogate_against_fp32c_and_without_the_network(trained):
     assert float(((got[nz] - out32[nz]).abs() / out32[nz]).max()) < 1.01e-3
     if s.process == 1:
         assert tsur < t32, (tsur, t32)
+
+
+def test_special_and_out_of_domain_inputs_like_the_reference(trained):
+    """NaN, infinities, zeros, negative values, pairs outside the trained
+    domain (K beyond [1e-3, 1e6] GeV) and pairs at kinematic edges take the
+    exact bounds and, through the model's trust grid, the FP32C fallback:
+    the NaN, infinity and zero patterns are the reference's and finite
+    values are within the bound."""
+    s = trained
+    K = np.array([np.nan, 1.0, np.inf, 0.0, 1.0, 10.0, -1.0, 1e6, 1e-3, 5e6, 1e-4, 2e7, 300.0, 1e9, 50.0])
+    q = np.array([1.0, np.nan, 1.0, 1e-3, 0.0, -1.0, 0.5, np.inf, 1e-3, 2e6, 5e-5, 1e7, 150.0, 4e8, 49.9])
+    counts = [0] * len(BATCH_Z)
+    counts[BATCH_Z.index(11)] = K.size
+    # pairs stored per element: all of them in standard rock's segment
+    tk, tq = torch.from_numpy(K).cuda(), torch.from_numpy(q).cuda()
+    out, st = s.infer(tk, tq, counts)
+    got = out.cpu().numpy()
+    exp = oracle.dcs(s.process, K, q, ELEMENTS[11], MUON_MASS)
+    assert np.array_equal(np.isnan(got), np.isnan(exp))
+    assert np.array_equal(np.isinf(got), np.isinf(exp))
+    fin = np.isfinite(exp)
+    assert np.array_equal(got[fin] == 0, exp[fin] == 0)
+    nz = fin & (exp != 0)
+    if nz.any():
+        assert float((np.abs(got[nz] - exp[nz]) / exp[nz]).max()) <= 1e-3
