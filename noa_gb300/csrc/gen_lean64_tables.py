@@ -55,13 +55,12 @@ def main():
     out.append(f"#define LEAN64_INV_LN2N {float(EXP_N / ln2)!r}")
     out.append(f"#define LEAN64_LN2N_HI {float(hi)!r}")
     out.append(f"#define LEAN64_LN2N_LO {float(lo)!r}")
-    out.append("/* 1/m_t rounded to float (1 for the two bins touching 1), stored as")
-    out.append("   double so that no float -> double conversion is needed. */")
-    out.append("static __device__ const double lean64_log_c[%d] = {" % len(c))
-    out.append(",\n".join("    %r" % v for v in c) + "};")
-    out.append("/* -log(c_t) rounded to double. */")
-    out.append("static __device__ const double lean64_log_l[%d] = {" % len(L))
-    out.append(",\n".join("    %s" % repr(v) for v in L) + "};")
+    out.append("/* Per bin t, {c_t, L_t}: c_t = 1/m_t rounded to float (1 for the two")
+    out.append("   bins touching 1), stored as double so that no float -> double")
+    out.append("   conversion is needed, and L_t = -log(c_t) rounded to double.  The")
+    out.append("   pair is one 16-byte entry: a single load per logarithm. */")
+    out.append("static __device__ const double2 lean64_log_cl[%d] = {" % len(c))
+    out.append(",\n".join("    {%r, %s}" % (a, repr(b)) for a, b in zip(c, L)) + "};")
     out.append("/* 2^(j/128) rounded to double. */")
     out.append("static __device__ const double lean64_exp_t[%d] = {" % len(T))
     out.append(",\n".join("    %s" % repr(v) for v in T) + "};")

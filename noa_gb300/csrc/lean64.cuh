@@ -72,8 +72,8 @@ __device__ __forceinline__ double lean_log(double x) {
     const int shift = t >= LEAN64_LOG_SPLIT ? 1 : 0;
     const int e = (hi >> 20) - 1023 + shift;
     const double m = __longlong_as_double((b & 0x000FFFFFFFFFFFFFLL) | ((long long)(1023 - shift) << 52));
-    const double c = __ldg(&lean64_log_c[t]);
-    const double L = __ldg(&lean64_log_l[t]);
+    const double2 cl = __ldg(&lean64_log_cl[t]);  // {c_t, L_t}, one 16-byte load
+    const double c = cl.x, L = cl.y;
     const double r = fma(m, c, -1.0);
     const float rf = fpconv::f32(r);
     const float t5 = fmaf(rf, fmaf(rf, 1.f / 7.f, -1.f / 6.f), 1.f / 5.f);
