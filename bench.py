@@ -745,7 +745,11 @@ def run_ours(args):
                                        "(profiles/traffic.json) x n / 1e7",
                      "peak_source": "FP64 FMA-chain probe (noa_dcs_probe_fma, libnoa_dcs_diag.so) measured in "
                                     "this run",
-                     "numerator": f"{FLOP_EQ_PER_EVAL[dom]} flop-eq/eval x {n} evals per launch"},
+                     "numerator": f"{FLOP_EQ_PER_EVAL[dom]} flop-eq/eval x {n} evals per launch",
+                     "convention": "flop-eq counted on the oracle, each libm log/exp/pow = 20; the kernels "
+                                   "compute log/exp/reciprocal mostly on the integer and FP32 pipes (1/2/0 FP64 "
+                                   "instructions), so frac can exceed 1; ncu pipe utilisation of the same kernel "
+                                   "in profiles/dcs_fp64_1e8.md"},
         "per_process": per_process,
         "variants": variants,
         "e2e": e2e,
