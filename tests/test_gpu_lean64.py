@@ -1,5 +1,8 @@
 """Error bounds of the FP64 elementary functions in lean64.cuh, measured on
-the GPU against the host libm (numpy, correctly rounded or within 1 ulp)."""
+the GPU against the host libm (numpy, correctly rounded or within 1 ulp).
+The functions themselves are within ~1.2 ulp of the exact value (log, exp)
+and 0.51 ulp (reciprocal), measured against long double in
+tests/test_lean64_host.py; the bars here allow numpy's own rounding."""
 import numpy as np
 import pytest
 import torch
@@ -34,7 +37,7 @@ def test_log(cuda_device):
     x = np.concatenate([sample(rng, 400000, 1e-300, 1e300), 1 + rng.uniform(-1e-2, 1e-2, 200000),
                         1 + rng.uniform(-1e-9, 1e-9, 50000), [1.0, 2.0, 0.5, np.sqrt(2.0)]])
     u = ulps(run(0, x), np.log(x))
-    assert u.max() <= 4.0, u.max()
+    assert u.max() <= 2.0, u.max()
     assert u.mean() <= 0.5
     special = np.array([0.0, -1.0, np.inf, np.nan, 5e-324, -0.0])
     got = run(0, special)
@@ -49,7 +52,7 @@ def test_exp(cuda_device):
     x = np.concatenate([rng.uniform(-699, 699, 400000), rng.uniform(-1e-3, 1e-3, 100000),
                         rng.uniform(-30, 30, 100000), [0.0, 1.0, -1.0]])
     u = ulps(run(1, x), np.exp(x))
-    assert u.max() <= 4.0, u.max()
+    assert u.max() <= 2.0, u.max()
     assert u.mean() <= 0.5
     special = np.array([800.0, -800.0, np.inf, -np.inf, np.nan])
     got = run(1, special)
@@ -62,10 +65,10 @@ def test_exp(cuda_device):
 def test_reciprocal_division_sqrt(cuda_device):
     rng = np.random.default_rng(3)
     b = sample(rng, 300000, 1e-300, 1e300) * rng.choice([-1.0, 1.0], 300000)
-    assert ulps(run(2, b), 1.0 / b).max() <= 2.0
+    assert ulps(run(2, b), 1.0 / b).max() <= 1.0
     a = sample(rng, 300000, 1e-100, 1e100)
     bd = sample(rng, 300000, 1e-150, 1e150) * rng.choice([-1.0, 1.0], 300000)   # a / b stays a normal double
-    assert ulps(run(3, a, bd), a / bd).max() <= 3.0
+    assert ulps(run(3, a, bd), a / bd).max() <= 2.0
     x = sample(rng, 300000, 1e-300, 1e300)
     assert ulps(run(4, x), np.sqrt(x)).max() <= 2.0
     special = np.array([0.0, -0.0, np.inf, -np.inf, np.nan, 5e-324])
