@@ -119,15 +119,15 @@ inline double exp_entry(int j) { return lean64_exp_t_host[j]; }
 #endif
 
 // f 2^F as a signed 64-bit integer, truncated toward zero; 0 for zero and
-// float subnormals.  Callers keep |f| 2^F below 2^55 (shift <= 31 here).
+// float subnormals.  Callers keep |f| 2^F below 2^55 (a left shift <= 31).
 LEAN64_FN long long fix_from_float(float f, int F) {
     const unsigned u = f2u(f);
-    const int ef = (int)((u >> 23) & 0xFFu);
-    const unsigned long long m = (unsigned long long)((u & 0x7FFFFFu) | 0x800000u);
-    const int sh = ef - 150 + F;  // the weight of the significand's bit 0 is 2^(ef - 150)
-    const int shl = sh < 0 ? 0 : (sh > 39 ? 39 : sh);
-    const int shr = sh > 0 ? 0 : (-sh > 63 ? 63 : -sh);
-    const unsigned long long v = ef == 0 ? 0ull : ((m << shl) >> shr);
+    const unsigned ef = (u >> 23) & 0xFFu;
+    // the significand (implicit bit set) at bits 40..63: the float's
+    // exponent and sign bits fall off the top of the word
+    const unsigned long long m = (unsigned long long)(u | 0x800000u) << 40;
+    const int t = 190 - (int)ef - F;  // bit 0 of the significand weighs 2^(ef - 150); t >= 9
+    const unsigned long long v = (ef != 0u && t < 64) ? (m >> t) : 0ull;
     return (u >> 31) ? -(long long)v : (long long)v;
 }
 
@@ -251,8 +251,11 @@ LEAN64_FN double lean_exp(double x) {
     const unsigned long long Mr = (br & 0x000FFFFFFFFFFFFFull) | (er ? 0x0010000000000000ull : 0ull);
     const int shr = 1005 - (int)(er ? er : 1u);  // the weight of bit 0 of Mr is 2^(er - 1075)
     const long long Pr = (long long)(shr <= 0 ? Mr << (-shr < 10 ? -shr : 10) : Mr >> (shr > 63 ? 63 : shr));
-    const long long S = (rs ? -Pr : Pr) + fix_from_float(dh, 70) + fix_from_float(dl, 70) -
-                        fix_from_float(kh, 70) - fix_from_float(kl, 70);
+    // d - k lo as one float pair (two-sum), then into the fixed-point sum
+    const float xs = fadd(dh, -kh);
+    const float xb = fadd(xs, -dh);
+    const float xl = fadd(fadd(fadd(dh, -fadd(xs, -xb)), fadd(-kh, -xb)), fadd(dl, -kl));
+    const long long S = (rs ? -Pr : Pr) + fix_from_float(xs, 70) + fix_from_float(xl, 70);
     const double p = S == 0 ? 0.0 : fix_to_double(S, 70);
     const double tj = exp_entry(k & (LEAN64_EXP_N - 1));
     const double y = fma(tj, p, tj);
