@@ -45,9 +45,10 @@ constexpr int CMP_TILE = CMP_THREADS * CMP_ITEMS;
 constexpr int CMP_QCAP = CMP_TILE + CMP_THREADS;
 
 // Resident CTAs per SM that the compacting kernels are compiled for (the
-// register budget per thread follows).  Measured on 1e7 pairs: pair
-// production 13.8 ms at 2 (112 registers) against 18.5 ms at 3; photonuclear
-// 9.0 ms at 4 (64 registers) against 10.8 ms at 3.
+// register budget per thread follows).  Measured on 1e8 pairs: pair
+// production 82.1 ms at 2 (108 registers) against 89.4 ms at 3 and 82.1 ms
+// at 1; photonuclear 45.0 ms at 4 (64 registers) against 47.6 ms at 3,
+// 45.2 ms at 5 and 46.0 ms at 2.
 #define NOA_DCS_PPROD_MIN_CTAS 2
 #define NOA_DCS_PHOTO_MIN_CTAS 4
 
