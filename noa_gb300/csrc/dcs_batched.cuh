@@ -69,6 +69,16 @@ __device__ __forceinline__ double batch_eval64(double K, double q, const noa_dcs
         return ion_fp64(K, q, c);
 }
 
+// The FP32C engine's FP64 redo: out of line for the two quadrature processes.
+template <int PROC>
+__device__ __forceinline__ double batch_redo64(double K, double q, const noa_dcs_consts &c) {
+    if (PROC == NOA_DCS_PROC_PPROD)
+        return pprod_fp64_ol(K, q, c);
+    else if (PROC == NOA_DCS_PROC_PHOTO)
+        return photo_fp64_ol(K, q, c);
+    return batch_eval64<PROC>(K, q, c);
+}
+
 template <int PROC>
 __device__ __forceinline__ double batch_eval32(double K, double q, const noa_dcs_consts &c, float &est) {
     if (PROC == NOA_DCS_PROC_BREMS)
@@ -265,7 +275,7 @@ __global__ void __launch_bounds__(THREADS) dcs_batched_kernel(const __grid_const
                                             (int)threadIdx.x < take, p.out, cc, p.tol);
                         } else if ((int)threadIdx.x < take) {
                             const int e = r - take + threadIdx.x;
-                            p.out[rI[e]] = batch_eval64<PROC>(rK[e], rQ[e], cc);
+                            p.out[rI[e]] = batch_redo64<PROC>(rK[e], rQ[e], cc);
                         }
                         __syncthreads();
                         if (threadIdx.x == 0)
@@ -280,7 +290,7 @@ __global__ void __launch_bounds__(THREADS) dcs_batched_kernel(const __grid_const
                         const int take = x < THREADS ? x : THREADS;
                         if ((int)threadIdx.x < take) {
                             const int e = x - take + threadIdx.x;
-                            p.out[xI[e]] = batch_eval64<PROC>(xK[e], xQ[e], cc);
+                            p.out[xI[e]] = batch_redo64<PROC>(xK[e], xQ[e], cc);
                         }
                         __syncthreads();
                         if (threadIdx.x == 0)

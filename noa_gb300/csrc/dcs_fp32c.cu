@@ -38,11 +38,12 @@ constexpr int F_QCAP = F_TILE + F_THREADS;
 constexpr int F_RCAP = 2 * F_THREADS;
 
 // Resident CTAs per SM that each kernel is compiled for (its register budget
-// follows).  Measured on 1e7 pairs: pair production is fastest at 2 (3.5 ms
-// at 3, where it spills), photonuclear at 3; the short bodies fit 4.
+// follows).  Measured on 1e8 pairs: pair production is fastest at 2 (12.1 ms;
+// 13.8 ms at 3, where it spills); photonuclear at 4 (4.32 ms against 4.60 ms
+// at 3), with its FP64 redo out of line; the short bodies fit 4.
 template <int PROC>
 constexpr int f32_min_ctas() {
-    return PROC == NOA_DCS_PROC_PPROD ? 2 : PROC == NOA_DCS_PROC_PHOTO ? 3 : 4;
+    return PROC == NOA_DCS_PROC_PPROD ? 2 : 4;
 }
 
 template <int PROC>
@@ -67,6 +68,17 @@ __device__ __forceinline__ double eval64(double K, double q, const noa_dcs_const
         return photo_fp64(K, q, c);
     else
         return ion_fp64(K, q, c);
+}
+
+// The FP64 redo: out of line for the two quadrature processes
+// (pprod_fp64_ol, photo_fp64_ol).
+template <int PROC>
+__device__ __forceinline__ double redo64(double K, double q, const noa_dcs_consts &c) {
+    if (PROC == NOA_DCS_PROC_PPROD)
+        return pprod_fp64_ol(K, q, c);
+    else if (PROC == NOA_DCS_PROC_PHOTO)
+        return photo_fp64_ol(K, q, c);
+    return eval64<PROC>(K, q, c);
 }
 
 template <int PROC>
@@ -251,7 +263,7 @@ __global__ void __launch_bounds__(F_THREADS, f32_min_ctas<PROC>()) dcs_fp32c_ker
                     fine_step<PROC>(s, rn - take + threadIdx.x, (int)threadIdx.x < take, out, c, tol);
                 } else if ((int)threadIdx.x < take) {
                     const int e = rn - take + threadIdx.x;
-                    out[s.rI[e]] = eval64<PROC>(s.rK[e], s.rQ[e], c);
+                    out[s.rI[e]] = redo64<PROC>(s.rK[e], s.rQ[e], c);
                 }
                 __syncthreads();
                 if (threadIdx.x == 0)
@@ -265,7 +277,7 @@ __global__ void __launch_bounds__(F_THREADS, f32_min_ctas<PROC>()) dcs_fp32c_ker
                     const int take = xn < F_THREADS ? xn : F_THREADS;
                     if ((int)threadIdx.x < take) {
                         const int e = xn - take + threadIdx.x;
-                        out[s.xI[e]] = eval64<PROC>(s.xK[e], s.xQ[e], c);
+                        out[s.xI[e]] = redo64<PROC>(s.xK[e], s.xQ[e], c);
                     }
                     __syncthreads();
                     if (threadIdx.x == 0)

@@ -352,6 +352,17 @@ __device__ __forceinline__ double photo_fp64(double K, double q, const noa_dcs_c
     return (ds < 0.) ? 0. : 0.5 * ds * dpQ2 * (mass + K) * c.scale_A;
 }
 
+// Out-of-line entries of the two quadrature bodies for the FP32C redo paths
+// (FP32C, batched FP32C and surrogate fallback kernels): the redo runs for
+// 0-0.5% of the open pairs, and inlined it would set the register budget of
+// the whole kernel.  Photonuclear's FP32C kernel runs 7% faster with it.
+static __device__ __noinline__ double pprod_fp64_ol(double K, double q, const noa_dcs_consts &c) {
+    return pprod_fp64(K, q, c);
+}
+static __device__ __noinline__ double photo_fp64_ol(double K, double q, const noa_dcs_consts &c) {
+    return photo_fp64(K, q, c);
+}
+
 // ---------------------------------------------------------------- ionisation
 __device__ __forceinline__ double ion_fp64(double K, double q, const noa_dcs_consts &c) {
     const double mass = c.mass;

@@ -362,7 +362,7 @@ __global__ void __launch_bounds__(256, 4) fallback_kernel(const __grid_constant_
                         if (!again)
                             p.out[j] = v;
                     } else {
-                        p.out[j] = noa_dcs::photo_fp64(p.K[j], p.q[j], c);
+                        p.out[j] = noa_dcs::photo_fp64_ol(p.K[j], p.q[j], c);
                     }
                 }
                 if (fine)
@@ -380,7 +380,7 @@ __global__ void __launch_bounds__(256, 4) fallback_kernel(const __grid_constant_
                     if ((int)threadIdx.x < take) {
                         const int k = nx - take + threadIdx.x;
                         const int32_t j = xq[k];
-                        p.out[j] = noa_dcs::pprod_fp64(p.K[j], p.q[j], p.consts[xs[k]]);
+                        p.out[j] = noa_dcs::pprod_fp64_ol(p.K[j], p.q[j], p.consts[xs[k]]);
                     }
                     __syncthreads();
                     if (threadIdx.x == 0)
