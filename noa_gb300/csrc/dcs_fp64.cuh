@@ -364,19 +364,49 @@ static __device__ __noinline__ double photo_fp64_ol(double K, double q, const no
 }
 
 // ---------------------------------------------------------------- ionisation
+// ionisation's first exit (dcs.hh:413-419: W_max < 5% K or q > W_max),
+// decided in float first: W_max = 2 me K (K + 2 mass) / ((mass + me)^2 +
+// 2 me K) has only positive terms, so its float value is within a few float
+// ulps; each bound is decided with a relative margin of 1e-5.  1: the exit is
+// not taken, 0: it is taken, -1: within a margin or outside the float-safe
+// range (zero, NaN, inf, huge), where the caller takes the exact IEEE test.
+// Only the decision is taken from float, never a value.
+__device__ __forceinline__ int ion_first_exit(double K, double q, const noa_dcs_consts &c) {
+    const float Kf = fpconv::f32_normal(K), qf = fpconv::f32_normal(q);  // NaN outside the normal range
+    if (!(Kf >= 1e-30f && Kf <= 1e15f && qf >= 1e-30f && qf <= 1e30f))
+        return -1;
+    constexpr float me = (float)NOA_ELECTRON_MASS;
+    const float W = 2.f * me * Kf * (Kf + 2.f * c.mass_h) / (c.io_cm_h + 2.f * me * Kf);
+    constexpr float lo = 0.99999f, hi = 1.00001f;
+    const float cut = (float)NOA_X_FRACTION * Kf;
+    if (W < cut * lo || qf > W * hi)
+        return 0;
+    return (W > cut * hi && qf < W * lo) ? 1 : -1;
+}
+
 __device__ __forceinline__ double ion_fp64(double K, double q, const noa_dcs_consts &c) {
     const double mass = c.mass;
     const double P2 = K * (K + 2. * mass);
     const double E = K + mass;
-    const double Wmax = ion_wmax(P2, E, c);
-    if ((Wmax < NOA_X_FRACTION * K) || (q > Wmax))
+    const int first = ion_first_exit(K, q, c);
+    double inv_Wmax;
+    if (first < 0) {
+        const double Wmax = ion_wmax(P2, E, c);
+        if ((Wmax < NOA_X_FRACTION * K) || (q > Wmax))
+            return 0.;
+        inv_Wmax = lean_rcp(Wmax);
+    } else if (first == 0) {
         return 0.;
+    } else {
+        // 1 / W_max = (mass^2 + me (me + 2 E)) / (2 me P2), lean
+        inv_Wmax = (mass * mass + ME * (ME + 2. * E)) * lean_rcp(2. * ME * P2);
+    }
     if (q <= c.io_Wmin)
         return 0.;
     const double inv_P2 = lean_rcp(P2);
     const double inv_q = lean_rcp(q);
     const double a0 = 0.5 * inv_P2;
-    const double a1 = -lean_rcp(Wmax);
+    const double a1 = -inv_Wmax;
     const double a2 = E * E * inv_P2;
     const double cs = c.io_cZA * E * (a0 + inv_q * (a1 + a2 * inv_q));
     double Delta = 0.;
