@@ -89,6 +89,7 @@ DIAG_PATH = os.path.join(os.path.dirname(os.path.abspath(__file__)), "libnoa_dcs
 DIAG_SIGNATURES = {
     "noa_dcs_probe_fma": (_INT, [_INT, _P, _INT, _INT, ctypes.POINTER(_D), _P]),
     "noa_dcs_lean64_eval": (_INT, [_INT, _P, _P, _P, _I64, _P]),
+    "noa_dcs_decision_check": (_INT, [_INT, _P, _P, _P, _I64, _D, _D, ctypes.c_int32, _D, _P]),
 }
 
 _lib = None

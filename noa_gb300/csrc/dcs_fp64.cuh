@@ -73,19 +73,24 @@ static __device__ __noinline__ double ol_rcp(double x) { return lean_rcp(x); }
 static __device__ __noinline__ double ol_div(double a, double b) { return lean_div(a, b); }
 
 // ---------------------------------------------------------------- bremsstrahlung
+// q < qe_max decides whether the electron term exists (physics.hh:142):
+// against a lean qe_max, and in IEEE arithmetic like the reference when q is
+// within 64 ulp of it.
+__device__ __forceinline__ bool brems_below(double E, double q, const noa_dcs_consts &c) {
+    const double qe_lean = E * lean_rcp(1. + c.br_half_m2 * lean_rcp(ME * E));
+    const long long dist = __double_as_longlong(q) - __double_as_longlong(qe_lean);
+    if (dist < 64 && dist > -64)
+        return brems_below_qe(E, q, c);
+    return q < qe_lean;
+}
+
 __device__ __forceinline__ double brems_fp64(double K, double q, const noa_dcs_consts &c) {
     const double mass = c.mass;
     const double sqrte = 1.648721271;
     const double E = K + mass;
     const double invE = lean_rcp(E);
     const double delta_factor = c.br_half_m2 * invE;
-    // q < qe_max decides whether the electron term exists (physics.hh:142);
-    // decided in IEEE arithmetic like the reference when q is within 64 ulp.
-    const double qe_lean = E * lean_rcp(1. + c.br_half_m2 * lean_rcp(ME * E));
-    bool below = q < qe_lean;
-    const long long dist = __double_as_longlong(q) - __double_as_longlong(qe_lean);
-    if (dist < 64 && dist > -64)
-        below = brems_below_qe(E, q, c);
+    const bool below = brems_below(E, q, c);
     const double nu = __ddiv_rn(q, E);  // as the reference: 1 - nu cancels as q -> E
     const double delta = delta_factor * nu * lean_rcp(1. - nu);
     const double Phi_n = clamp0(lean_log(c.br_BZ_n * (mass + delta * c.br_Dn_sqrte_m2) *

@@ -31,6 +31,17 @@ int noa_dcs_probe_fma(int fp64, void *out, int blocks, int iters, double *flops,
  * the casts. */
 int noa_dcs_lean64_eval(int fn, const double *x, const double *y, double *out, int64_t n, void *stream);
 
+/* out[i] for the pair (K[i], q[i]) of process proc (0 bremsstrahlung, 1 pair
+ * production, 2 photonuclear, 3 ionisation) on element (A, I, Z) and mass: the
+ * decision the DCS kernels take first in float or lean arithmetic --
+ * bremsstrahlung's electron term (q < qe_max), pair production's and
+ * photonuclear's open / closed, ionisation's first exit -- as 1 or 0 when it
+ * equals the reference's exact IEEE decision, -2 when it does not, and -1
+ * where ionisation's float test leaves the decision to the exact one.
+ * Device buffers; enqueued on `stream`. */
+int noa_dcs_decision_check(int proc, const double *K, const double *q, double *out, int64_t n, double A, double I,
+                           int32_t Z, double mass, void *stream);
+
 #ifdef __cplusplus
 }
 #endif
