@@ -204,7 +204,7 @@ const char *noa_dcs_batch_last_error(void);
  * serialised by the caller.  Set-up on the first call on each device: the
  * array's device address is looked up with that device current, and for
  * FP32C pair production (54 KB of shared memory) the kernel's shared-memory
- * limit is raised; make that first call before any stream capture.  Tile
+ * limit is raised; later calls make no runtime set-up call.  Tile
  * shape is fixed (256 threads x 4 pairs, 2 CTAs per SM).  Buffers as for the
  * plan. */
 int noa_dcs_cuda_vmap_batched_noalloc(int process, int precision, int n_segments, const noa_dcs_element *elements,
