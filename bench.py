@@ -815,7 +815,7 @@ def summarise(line):
         s["fp64_vs_oracle"] = {k: {"mean": _r(v["mean_rel"], 2), "max": _r(v["max_rel"], 2),
                                    "cond_ratio": _r(v["cond_ratio"], 2), "zeros_equal": v["zero_pattern_equal"]}
                                for k, v in par.items() if isinstance(v, dict)}
-    f = line["variants"].get("fp32c")
+    f = (line.get("variants") or {}).get("fp32c")
     if f:
         s["fp32c"] = {k: {"x_fp64": _r(v["speedup_vs_fp64"], 3), "max": _r(v["max_rel"], 2),
                           "median": _r(v["median_rel"], 2)} for k, v in f.items() if k in PROCESSES}

@@ -60,3 +60,20 @@ def test_summary_is_last_and_compact():
     text = json.dumps(line)
     assert list(json.loads(text))[-1] == "summary"
     assert len(json.dumps(line["summary"])) < 2500
+
+
+def test_hardware_roofline_view():
+    """roofline.hw_view: ncu's pipe utilisations of each FP64 kernel, from the
+    committed capture summary (profiles/traffic.json), the FP64 pipe as the
+    bound; the summary carries its fraction."""
+    for p in bench.PROCESSES:
+        hw = bench.hw_view(p)
+        assert hw is not None and hw["bound"] == "fp64 pipe", p
+        assert 0.0 < hw["frac"] <= 1.0 and hw["frac"] == hw["pipes"]["fp64_pipe"]
+        assert set(hw["pipes"]) == {"fp64_pipe", "alu_pipe", "fma_pipe", "issue"}
+        assert "profiles/" in hw["source"]
+    assert bench.hw_view("no such process") is None
+    line = {"value": 2.8e9, "config": bench.config_dict(100_000_000, 1), "e2e": None,
+            "roofline": {"frac": 1.16, "hw_view": bench.hw_view("pair_production")}}
+    s = bench.summarise(line)
+    assert s["fp64_pipe_frac"] == round(bench.hw_view("pair_production")["frac"], 3)
