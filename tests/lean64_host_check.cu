@@ -3,7 +3,10 @@
 // against long double libm.  Prints one line per input set:
 //   <set> <count> <max ulp> <mean ulp>
 // and one line per special value: special <fn> <x> <got> <expected>.
-// Built and run by tests/test_lean64_host.py.
+// Built and run by tests/test_lean64_host.py.  With arguments
+// `values <in> <out>` it instead reads n doubles (raw) from <in> and writes
+// lean_log(x) then lean_exp(x) for each (2n raw doubles) to <out>, for the
+// device-equals-host test in tests/test_gpu_lean64.py.
 #include <cmath>
 #include <cstdint>
 #include <cstdio>
@@ -46,7 +49,35 @@ double from_bits(uint64_t b) {
 
 } // namespace
 
+int values(const char *in, const char *out) {
+    FILE *f = std::fopen(in, "rb");
+    if (!f)
+        return 1;
+    std::fseek(f, 0, SEEK_END);
+    const long n = std::ftell(f) / 8;
+    std::fseek(f, 0, SEEK_SET);
+    double *x = new double[n], *y = new double[2 * n];
+    const long got = (long)std::fread(x, 8, n, f);
+    std::fclose(f);
+    if (got != n)
+        return 1;
+    for (long i = 0; i < n; i++) {
+        y[i] = lean64::lean_log(x[i]);
+        y[n + i] = lean64::lean_exp(x[i]);
+    }
+    FILE *o = std::fopen(out, "wb");
+    if (!o)
+        return 1;
+    const long put = (long)std::fwrite(y, 8, 2 * n, o);
+    std::fclose(o);
+    delete[] x;
+    delete[] y;
+    return put == 2 * n ? 0 : 1;
+}
+
 int main(int argc, char **argv) {
+    if (argc == 4 && std::strcmp(argv[1], "values") == 0)
+        return values(argv[2], argv[3]);
     const long n = argc > 1 ? std::atol(argv[1]) : 200000;
     std::mt19937_64 g(20240613);
     std::uniform_real_distribution<double> U(0, 1);

@@ -166,3 +166,38 @@ def test_float_float_log(cuda_device):
     big = np.abs(ref) > 0.1
     assert (err[big] / np.abs(ref[big]).astype(np.float64)).max() <= 5e-13
     assert err[~big].max() <= 3e-14
+
+
+def test_device_equals_host_build(cuda_device, tmp_path):
+    """lean_log and lean_exp on the GPU give the bits of the same source
+    compiled for the host (tests/lean64_host_check.cu, `values` mode) on
+    their fast paths (positive normal x for log, |x| < 700 for exp): the
+    functions are integer and float arithmetic with explicit FMAs, so the
+    host accuracy study (tests/test_lean64_host.py) describes the device
+    code exactly."""
+    import os
+    import shutil
+    import subprocess
+    nvcc = shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"
+    if not os.path.exists(nvcc):
+        pytest.skip("nvcc not available")
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    exe = str(tmp_path / "lean64_host_check")
+    subprocess.run([nvcc, "-std=c++17", "-O2", "-Xcompiler", "-ffp-contract=off", "-o", exe,
+                    os.path.join(root, "tests", "lean64_host_check.cu")], check=True, capture_output=True)
+    rng = np.random.default_rng(17)
+    raw = rng.integers(0, 1 << 63, 300_000, dtype=np.uint64).view(np.float64)
+    x = np.concatenate([raw[np.isfinite(raw)], sample(rng, 300_000, 1e-300, 1e300), rng.uniform(-745, 745, 300_000),
+                        1 + rng.uniform(-1e-3, 1e-3, 100_000), [0.0, -0.0, 1.0, 2.0, np.inf, -np.inf, np.nan]])
+    fin, fout = str(tmp_path / "x.bin"), str(tmp_path / "y.bin")
+    x.tofile(fin)
+    subprocess.run([exe, "values", fin, fout], check=True, timeout=600)
+    host = np.fromfile(fout, dtype=np.float64)
+    hlog, hexp = host[:x.size], host[x.size:]
+    # the fast paths (outside them each build calls its own platform's libm)
+    fast = {0: np.isfinite(x) & (x >= 2.0 ** -1022), 1: np.abs(x) < 700}
+    for fn, h in ((0, hlog), (1, hexp)):
+        d = run(fn, x)
+        m = fast[fn]
+        same = _bits(d[m]) == _bits(h[m])
+        assert m.sum() > 500_000 and same.all(), (fn, int((~same).sum()), x[m][~same][:5])
